@@ -1,0 +1,91 @@
+"""Pin the CPU oracle against the reference's own outputs (tests/golden/).
+
+The fixtures were produced by running the reference implementation
+(skelfmm/recursive_skel.py, skelfmm/batched_fmm.py, skelfmm/util.py,
+skelfmm/util_batched.py) on this framework's tree; see make_golden.py.
+"""
+import numpy as np
+import pytest
+
+from golden_util import OPNAME, build_cases, load_build, load_groups, relinf
+from oracle import skel_oracle as O
+from skelfmm_gb300.tree import BalancedTree
+
+LIST_KEYS = [
+    "leaf_uskel_from_qskel_list", "tree_uskel_from_qskel_list", "uskel_from_q_list",
+    "u_from_qskel_list", "u_from_q_list", "root_boxes", "skel_leaves", "short_vec_inds",
+    "long_vec_inds", "box_skel_inds", "child_skel_inds", "inds_lev_offset", "tree_boxes",
+    "tree_lev_sep", "nproxy_level",
+]
+
+
+def _oracle_build(d):
+    op = O.OPERATORS[OPNAME[str(d["operator"])]]
+    tree = BalancedTree(d["points"], int(d["leaf_size"]))
+    geom = d.get("geometry")
+    b = O.OracleBuild(tree, op, float(d["kappa"]), float(d["tol"]), geometry=geom)
+    return b.skel_tree(int(d["npoints_max"]))
+
+
+@pytest.mark.parametrize("name", build_cases())
+def test_oracle_build_matches_reference(name):
+    d = load_build(name)
+    b = _oracle_build(d)
+    assert b.root_level == int(d["root_level"])
+    assert np.array_equal(b.bs_list, d["bs_list"])
+    assert np.array_equal(b.rank_list, d["rank_list"])
+    assert b.min_rank == int(d["min_rank"]) and b.max_rank == int(d["max_rank"])
+    assert np.array_equal(b.XX_list(), d["XX_list"][:, : b.max_bs])
+    pl, pt = b.proj_lists()
+    for mine, ref in ((pl, d["proj_list"]), (pt, d["proj_list_tree"])):
+        scale = max(1.0, float(np.abs(ref).max()) if ref.size else 1.0)
+        assert mine.shape == ref.shape
+        assert np.allclose(mine, ref, rtol=1e-9, atol=1e-9 * scale)
+    for k in LIST_KEYS:
+        assert np.array_equal(np.asarray(getattr(b, k)), d[k]), k
+
+
+@pytest.mark.parametrize("name", build_cases())
+def test_oracle_apply_matches_reference(name):
+    d = load_build(name)
+    b = _oracle_build(d)
+    y = O.OracleApply(b, nthreads=2).matvec(d["x"])
+    # torch's bessel_j0/y0 (reference, helmholtz_2d) and scipy's differ near 1e-10
+    tol = 1e-9 if str(d["operator"]) == "HELMHOLTZ_2D" else 1e-12
+    assert relinf(y, d["y_batched"]) < tol
+    if "y_serial" in d:
+        assert relinf(y, d["y_serial"]) < 1e-12
+    assert relinf(y[d["dense_idx"]], d["y_dense"]) < max(10 * float(d["tol"]), 1e-12)
+
+
+def test_oracle_kernels_match_reference_blocks():
+    groups = load_groups("kernels.npz")
+    fn = {
+        "laplace_2d": "laplace_2d", "laplace_3d": "laplace_3d", "helmholtz_2d": "helmholtz_2d",
+        "helmholtz_3d": "helmholtz_3d", "laplace_3d_double_layer": "laplace_double_layer_3d",
+        "laplace_3d_adjoint_double_layer": "laplace_adjoint_double_layer_3d",
+        "helmholtz_3d_double_layer": "helmholtz_double_layer_3d",
+        "helmholtz_3d_adjoint_double_layer": "helmholtz_adjoint_double_layer_3d",
+    }
+    assert len(groups) == 32
+    for key, g in groups.items():
+        kname, m, case = key.split("/")
+        op = O.OPERATORS[fn[kname]]
+        geom = g.get("geom")
+        K = op.matrix(g["x"], g["y"], geom_trg=geom, geom_src=geom, param=float(g["kappa"]))
+        if case == "self":
+            np.fill_diagonal(K, 0.0)
+        tol = 1e-9 if kname == "helmholtz_2d" else 1e-10
+        assert relinf(K @ g["q"], g["out"]) < tol, key
+
+
+def test_oracle_id_matches_reference():
+    groups = load_groups("ids.npz")
+    for opname, g in groups.items():
+        op = O.OPERATORS[OPNAME[opname]]
+        rank, idx, proj = O.skel_box(op, float(g["kappa"]), g["x"], g["center"], float(g["length"]),
+                                     float(g["tol"]), int(g["nproxy"]), geom=g.get("geom"))
+        assert rank == int(g["rank"])
+        assert np.array_equal(idx, g["idx"])
+        if proj.size:
+            assert relinf(proj, g["proj"]) < 1e-8
