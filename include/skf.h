@@ -1,0 +1,151 @@
+/*
+ * skf.h — C ABI of the GB300 strong-recursive-skeletonization FMM.
+ *
+ * Every entry point returns an int status (SKF_OK = 0).  Device pointers are
+ * borrowed for the duration of the call; a plan owns the device buffers it
+ * allocates.  One plan must not be used from two host threads at once;
+ * different plans may run concurrently on different streams.
+ *
+ * Reference interfaces each call replaces (annayesy/skelFMM, Python):
+ *   skf_plan_create     SkelFMMBatched.build_from_copy   skelfmm/batched_fmm.py:92-174
+ *   skf_plan_apply      SkelFMMBatched.matvec            skelfmm/batched_fmm.py:539-564
+ *   skf_kernel_apply    KernelOperator.torch_apply       skelfmm/operators.py:69-89
+ *                       (the kernel_apply seam, skelfmm/batched_fmm.py:21-44,180-217)
+ *   skf_skel_boxes      util.skel_box_helper over a level skelfmm/util.py:381-437,
+ *                       driven by RecursiveSkeletonization.skel_tree
+ *                       skelfmm/recursive_skel.py:412-492
+ */
+#ifndef SKF_H
+#define SKF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SKF_OK 0
+#define SKF_ERR_ARG 1         /* bad argument / shape (ValueError in the reference) */
+#define SKF_ERR_OOM 2         /* device allocation failed */
+#define SKF_ERR_CUDA 3        /* a CUDA runtime call failed */
+#define SKF_ERR_UNSUPPORTED 4 /* operator/precision combination not built */
+#define SKF_ERR_ID 5          /* interpolative decomposition failed (non-finite input) */
+#define SKF_ERR_TIMEOUT 6     /* a bounded device-side wait ran out */
+
+/* operators (skelfmm/operators.py:159-216) */
+#define SKF_LAPLACE_2D 0
+#define SKF_LAPLACE_3D 1
+#define SKF_HELMHOLTZ_2D 2
+#define SKF_HELMHOLTZ_3D 3
+#define SKF_LAPLACE_DOUBLE_LAYER_3D 4
+#define SKF_LAPLACE_ADJOINT_DOUBLE_LAYER_3D 5
+#define SKF_HELMHOLTZ_DOUBLE_LAYER_3D 6
+#define SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D 7
+#define SKF_NUM_OPS 8
+
+/* apply precision */
+#define SKF_PREC_FP64 0  /* everything in FP64 */
+#define SKF_PREC_MIXED 1 /* FP32 kernel evaluation (FP64 tile sums), FP32 T/T^T */
+
+/* translation kinds in a target box's interaction list */
+#define SKF_KIND_COLLEAGUE 0   /* u += K q ; uskel[:r_u] -= K[:r_u,:r_s] qskel[:r_s] */
+#define SKF_KIND_COARSE_UP 1   /* u += K q ; uskel[:r_u] -= K[:r_u,:] q            */
+#define SKF_KIND_COARSE_DOWN 2 /* u += K q - K[:, :r_s] qskel[:r_s]                */
+#define SKF_KIND_ROOT 3        /* u += K q (dense root level)                       */
+
+typedef struct skf_plan skf_plan;
+
+/*
+ * A built skeletonization in ragged (CSR) form.  "Entries" are the points a
+ * box holds at its own level (leaf points, or the union of its children's
+ * skeletons), in the box's skeleton-first order.  All pointers are HOST
+ * pointers; skf_plan_create copies what it needs to the device.
+ */
+typedef struct {
+  int32_t op;          /* SKF_* operator id */
+  int32_t ndim;        /* 2 or 3 */
+  double kappa;        /* wavenumber (0 for Laplace) */
+  int64_t npoints;     /* N, length of the apply's input/output vectors */
+  int32_t nboxes;
+  int32_t nlevels;
+  int32_t root_level;
+  const int32_t* box_level; /* [nboxes] */
+  const int64_t* box_off;   /* [nboxes+1] entry offsets */
+  const int32_t* box_rank;  /* [nboxes] skeleton size (0 = not compressed) */
+  const double* entry_xyz;  /* [E*ndim] coordinates of every entry */
+  const double* entry_geom; /* [E*3] normals of every entry, or NULL */
+  const int64_t* entry_pslot; /* [E] entry index in the parent box of each skeleton
+                                 entry of a box below the root level, else -1 */
+  int64_t nperm;               /* number of (entry, point) pairs = N */
+  const int64_t* perm_entry;   /* [nperm] leaf entries ...            */
+  const int64_t* perm_point;   /* [nperm] ... and the point each holds */
+  const int64_t* t_off;        /* [nboxes] element offset of box T, or -1 */
+  const double* t_data;        /* T blocks, row-major rank x (bs-rank);
+                                  complex operators: interleaved (re,im) */
+  int64_t t_len;               /* number of scalars in t_data (complex: pairs) */
+  const int64_t* list_off;     /* [nboxes+1] per-target interaction lists */
+  const int32_t* list_src;     /* [L] source box */
+  const int8_t* list_kind;     /* [L] SKF_KIND_* */
+} skf_plan_desc;
+
+typedef struct {
+  int64_t nentries;
+  int64_t npairs_fused;   /* kernel evaluations per apply (translations) */
+  int64_t t_scalars;      /* scalars in all T blocks */
+  int64_t device_bytes;   /* bytes the plan holds on the device */
+  int32_t nwork;          /* translation work items */
+  int32_t is_complex;
+} skf_plan_info;
+
+int skf_plan_create(const skf_plan_desc* desc, skf_plan** out);
+int skf_plan_destroy(skf_plan* plan);
+int skf_plan_query(const skf_plan* plan, skf_plan_info* info);
+
+/* y = A x with the built operator.  x, y: DEVICE pointers to npoints FP64
+   (complex operators: interleaved complex128).  stream: cudaStream_t or NULL. */
+int skf_plan_apply(skf_plan* plan, const void* x, void* y, int32_t precision, void* stream);
+
+/* Same product with HOST buffers: copies x in, applies, copies y out, and
+   synchronises the stream before returning. */
+int skf_plan_apply_host(skf_plan* plan, const void* x_host, void* y_host, int32_t precision, void* stream);
+
+/* Time the plan's translation kernel alone (device time in ms over `reps`
+   launches, measured with events on `stream`).  For roofline reporting. */
+int skf_plan_time_translations(skf_plan* plan, int32_t precision, int32_t reps, void* stream, float* ms_out);
+
+/*
+ * Batched kernel-block products (the reference's kernel_apply seam):
+ * for pair p: out[p, 0:m[p]] = K(xt[p], xs[p]) @ q[p, 0:n[p]], with the
+ * diagonal zeroed when self_flag[p] != 0.  Points padded to mmax / nmax per
+ * pair, coordinates [npairs, mmax|nmax, ndim]; geometry [.., 3] or NULL.
+ * All DEVICE pointers, FP64 (complex: interleaved).  precision as above.
+ */
+int skf_kernel_apply(int32_t op, double kappa, int32_t npairs, int32_t mmax, int32_t nmax,
+                     const int32_t* m, const int32_t* n, const double* xt, const double* xs,
+                     const double* gt, const double* gs, const void* q, const int8_t* self_flag,
+                     void* out, int32_t precision, void* stream);
+
+/*
+ * Proxy-surface interpolative decompositions of a batch of boxes
+ * (one level of the build).  For box b: points xb = x[off[b]:off[b+1]] (DEVICE,
+ * [.., ndim] FP64), geometry likewise or NULL, box centre centers[b*ndim..],
+ * side length `box_length`, `nproxy` requested proxy points, tolerance `tol`
+ * (relative, < 1) or fixed rank (>= 1).
+ * Outputs (DEVICE): rank[b]; perm[off[b]:off[b+1]] (skeleton first, local
+ * indices); T written at t_out + t_off_out[b] as rank x (bs-rank) row-major,
+ * where t_off_out[b] = sum over earlier boxes of bs*bs (capacity bound).
+ */
+int skf_skel_boxes(int32_t op, double kappa, int32_t nbox, const int64_t* off, const double* x,
+                   const double* geom, const double* centers, double box_length, int32_t nproxy,
+                   double tol, int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out,
+                   void* stream);
+
+const char* skf_status_string(int32_t status);
+int skf_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKF_H */

@@ -256,6 +256,55 @@ def skel_box(op, kappa, x_box, center, box_length, tol, nproxy, geom=None):
     return pivoted_qr_id(K, tol)
 
 
+def _skel_task(args):
+    """Pool worker: one box's proxy ID (util.py:381-402), single-threaded BLAS."""
+    opname, kappa, xb, c, len_l, tol, nproxy, gb = args
+    try:
+        from threadpoolctl import threadpool_limits
+    except ImportError:  # pragma: no cover
+        return skel_box(OPERATORS[opname], kappa, xb, c, len_l, tol, nproxy, geom=gb)
+    with threadpool_limits(limits=1):
+        return skel_box(OPERATORS[opname], kappa, xb, c, len_l, tol, nproxy, geom=gb)
+
+
+def translation_sample(op_name, kappa, entry_xyz, entry_geom, box_off, box_rank, list_off, list_src,
+                       list_kind, q, qh, boxes, nthreads=None):
+    """Dense CPU translations (FP64, kernel blocks materialised as the
+    reference's batched path does, batched_fmm.py:180-302) into the target
+    boxes ``boxes`` of a ragged build.  Returns (u, uh, pair evaluations)
+    per box; used to time the reference algorithm on a bounded sample."""
+    op = OPERATORS[op_name]
+
+    def one(U):
+        oU, eU = int(box_off[U]), int(box_off[U + 1])
+        rU = int(box_rank[U])
+        XU = entry_xyz[oU:eU]
+        GU = None if entry_geom is None else entry_geom[oU:eU]
+        au = np.zeros(eU - oU, q.dtype)
+        ah = np.zeros(eU - oU, q.dtype)
+        npairs = 0
+        for l in range(int(list_off[U]), int(list_off[U + 1])):
+            s, kind = int(list_src[l]), int(list_kind[l])
+            oS, eS = int(box_off[s]), int(box_off[s + 1])
+            rS = int(box_rank[s])
+            GS = None if entry_geom is None else entry_geom[oS:eS]
+            K = op.matrix(XU, entry_xyz[oS:eS], geom_trg=GU, geom_src=GS, param=kappa)
+            if U == s:
+                np.fill_diagonal(K, 0.0)
+            npairs += K.size
+            au += K @ q[oS:eS]
+            if kind == 0:
+                ah[:rU] -= K[:rU, :rS] @ qh[oS:oS + rS]
+            elif kind == 1:
+                ah[:rU] -= K[:rU] @ q[oS:eS]
+            elif kind == 2:
+                au -= K[:, :rS] @ qh[oS:oS + rS]
+        return au, ah, npairs
+
+    with ThreadPoolExecutor(nthreads or max(1, os.cpu_count() or 1)) as ex:
+        return list(ex.map(one, list(boxes)))
+
+
 def nproxy_levels(ndim, tol, kappa, L0, nlevels):
     """recursive_skel.py:72-85."""
     ndigits = int(-np.log10(tol / 100))
@@ -325,8 +374,10 @@ class OracleBuild:
             self.pid[box] = np.concatenate(parts) if parts else np.zeros(0, int)
             self.bs_list[box] = self.pid[box].shape[0]
 
-    def skel_tree(self, npoints_max):
-        """recursive_skel.py:326-502 (serial branch)."""
+    def skel_tree(self, npoints_max, pool=None):
+        """recursive_skel.py:326-502.  ``pool``: an optional process pool
+        (``multiprocessing`` spawn context, as the reference's ``p="auto"``)
+        that takes the boxes of a level; otherwise serial."""
         tree = self.tree
         self.root_level = max(0, tree.nlevels - 1)
         for lev in range(tree.nlevels - 1, 0, -1):
@@ -339,13 +390,18 @@ class OracleBuild:
             len_l = tree.get_box_length(boxes_lev[0])
             centers = tree.get_boxes_centers(boxes_lev)
             nproxy = int(self.nproxy_level[lev])
+            tasks = []
             for box, c in zip(boxes_lev, centers):
                 ids = self.pid[box]
-                xb = tree.XX[ids]
                 gb = None if self.geometry is None else self.geometry[ids]
-                rank, idx, proj = skel_box(self.op, self.kappa, xb, c, len_l, self.tol, nproxy, geom=gb)
+                tasks.append((self.op.name, self.kappa, tree.XX[ids], c, len_l, self.tol, nproxy, gb))
+            if pool is None:
+                results = map(_skel_task, tasks)
+            else:
+                results = pool.imap(_skel_task, tasks, chunksize=max(1, len(tasks) // 64))
+            for box, (rank, idx, proj) in zip(boxes_lev, results):
                 self.rank_list[box] = rank
-                self.pid[box] = ids[idx]
+                self.pid[box] = self.pid[box][idx]
                 self.proj[box] = proj
         self._finish()
         return self

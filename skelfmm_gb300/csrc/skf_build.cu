@@ -1,0 +1,537 @@
+// skf_build.cu — proxy-surface interpolative decompositions of one tree level.
+//
+// Replaces util.skel_box_helper (skelfmm/util.py:404-437) as driven by
+// RecursiveSkeletonization.skel_tree (skelfmm/recursive_skel.py:412-492):
+// for every box of a level, in one launch (one thread block per box),
+//   1. the stacked proxy matrix (util.py:87-124): symmetric point kernels use
+//      K(x_box, proxy)^T (nproxy x bs) — the reference stacks that block twice,
+//      which scales R by sqrt(2) and leaves ranks, pivots and T unchanged —
+//      geometry kernels use [K(proxy, x_box); K(x_box, proxy)^T] (2 nproxy x bs);
+//   2. a column-pivoted Householder QR in FP64 (Businger & Golub, 1965) with
+//      the partial-norm downdating safeguard of Drmac & Bujanovic (LAPACK
+//      Working Note 176), stopped at the first |R_kk| <= tol |R_00|
+//      (util.py:25-35 counts |R_ii| > tol |R_00|; the diagonal of a
+//      column-pivoted QR is non-increasing);
+//   3. T = R11^{-1} R12 by column-oriented back substitution (util.py:41-49).
+// The proxy matrix lives column-major in a global workspace (L2-resident for
+// leaf-sized boxes); one warp owns a column during each trailing update.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "skf_internal.cuh"
+#include "skf_kernels.cuh"
+
+namespace skf {
+
+// Proxy surfaces of side 1 centred at the origin, matching
+// skelfmm_gb300.tree.get_cube_surface / get_sphere_surface.
+static std::vector<double> proxy_template(int ndim, bool sphere, int nproxy) {
+  std::vector<double> t;
+  const double length = 1.0, h = 0.5;
+  if (!sphere) {
+    if (ndim == 2) {
+      const int n = std::max(1, (int)std::ceil(nproxy / 4.0));
+      for (int side = 0; side < 4; ++side)
+        for (int k = 0; k < n; ++k) {
+          const double s = -h + length * (double)k / n;
+          double x = 0, y = 0;
+          if (side == 0) { x = s; y = -h; }
+          if (side == 1) { x = h; y = s; }
+          if (side == 2) { x = -s; y = h; }
+          if (side == 3) { x = -h; y = -s; }
+          t.push_back(x);
+          t.push_back(y);
+        }
+    } else {
+      const int n = std::max(1, (int)std::ceil(std::sqrt(nproxy / 6.0)));
+      for (int axis = 0; axis < 3; ++axis) {
+        int o0 = axis == 0 ? 1 : 0, o1 = axis == 2 ? 1 : 2;
+        for (int sg = 0; sg < 2; ++sg)
+          for (int a = 0; a < n; ++a)
+            for (int b = 0; b < n; ++b) {
+              double p[3];
+              p[axis] = sg == 0 ? -h : h;
+              p[o0] = -h + length * (a + 0.5) / n;
+              p[o1] = -h + length * (b + 0.5) / n;
+              t.push_back(p[0]);
+              t.push_back(p[1]);
+              t.push_back(p[2]);
+            }
+      }
+    }
+  } else {
+    const int n = std::max(1, nproxy);
+    if (ndim == 2) {
+      for (int k = 0; k < n; ++k) {
+        const double th = 2.0 * M_PI * k / n;
+        t.push_back(h * std::cos(th));
+        t.push_back(h * std::sin(th));
+      }
+    } else {
+      const double ga = M_PI * (3.0 - std::sqrt(5.0));
+      for (int k = 0; k < n; ++k) {
+        const double kk = k + 0.5;
+        const double z = 1.0 - 2.0 * kk / n;
+        const double rho = std::sqrt(std::max(0.0, 1.0 - z * z));
+        const double phi = ga * kk;
+        t.push_back(h * rho * std::cos(phi));
+        t.push_back(h * rho * std::sin(phi));
+        t.push_back(h * z);
+      }
+    }
+  }
+  return t;
+}
+
+struct SkelArgs {
+  const int64_t* off;
+  const double* x;
+  const double* geom;
+  const double* centers;
+  const double* tmpl;  // [np * ndim] unit proxy surface
+  int np;              // proxy points
+  int mrows;           // rows of the proxy matrix (np or 2 np)
+  double plen;         // proxy side = 2.95 * box length
+  double kappa;
+  double tol;
+  double* ws;          // column-major workspace
+  const int64_t* ws_off;
+  int32_t* rank;
+  int32_t* perm;
+  const int64_t* t_off_out;
+  double* t_out;
+  int first_box;
+};
+
+constexpr int kSkelThreads = 256;
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  v = warp_sum_d(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double s = 0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+  return s;
+}
+
+template <int OP>
+__global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
+  constexpr bool C = OpTraits<OP>::kComplex;
+  constexpr int D = OpTraits<OP>::kDim;
+  constexpr int G = OpTraits<OP>::kGeom;
+  constexpr int W = C ? 2 : 1;  // scalars per matrix entry
+  extern __shared__ double sm[];
+  const int b = a.first_box + blockIdx.x;
+  const int64_t off = a.off[b];
+  const int n = (int)(a.off[b + 1] - off);
+  const int m = a.mrows;
+  // smem: vn1[n], vn2[n], v[m*W], red[64], misc
+  double* vn1 = sm;
+  double* vn2 = vn1 + n;
+  double* vv = vn2 + n;
+  double* red = vv + (size_t)m * W;
+  int* piv = reinterpret_cast<int*>(red + 64);
+  __shared__ int s_k;
+  __shared__ double s_scal[4];
+
+  double* A = a.ws + a.ws_off[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double c[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
+
+  // ---- 1. proxy matrix, column j = box point j
+  for (int64_t idx = threadIdx.x; idx < (int64_t)m * n; idx += blockDim.x) {
+    const int j = (int)(idx / m), i = (int)(idx % m);
+    const double* xj = a.x + (off + j) * D;
+    const int pi = (i < a.np) ? i : i - a.np;
+    double p[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) p[d] = c[d] + a.plen * a.tmpl[pi * D + d];
+    double gx = 0, gy = 0, gz = 0;
+    double kr, ki;
+    // proxy normals (sphere proxies) are radial
+    double pn[3] = {0, 0, 0};
+    if (G != 0) {
+      double nn = 0;
+      for (int d = 0; d < D; ++d) {
+        pn[d] = p[d] - c[d];
+        nn += pn[d] * pn[d];
+      }
+      nn = sqrt(nn);
+      for (int d = 0; d < D; ++d) pn[d] /= nn;
+    }
+    if (G == 0 || i >= a.np) {
+      // K(x_j, p_i): target = box point, source = proxy
+      if (G == 1) { gx = pn[0]; gy = pn[1]; gz = pn[2]; }
+      if (G == 2) {
+        const double* g = a.geom + (off + j) * 3;
+        gx = g[0]; gy = g[1]; gz = g[2];
+      }
+      eval_f64<OP>(xj[0] - p[0], xj[1] - p[1], D == 3 ? xj[2] - p[2] : 0.0, gx, gy, gz, a.kappa, kr, ki);
+    } else {
+      // K(p_i, x_j): target = proxy, source = box point
+      if (G == 1) {
+        const double* g = a.geom + (off + j) * 3;
+        gx = g[0]; gy = g[1]; gz = g[2];
+      }
+      if (G == 2) { gx = pn[0]; gy = pn[1]; gz = pn[2]; }
+      eval_f64<OP>(p[0] - xj[0], p[1] - xj[1], D == 3 ? p[2] - xj[2] : 0.0, gx, gy, gz, a.kappa, kr, ki);
+    }
+    A[((int64_t)j * m + i) * W] = kr;
+    if (C) A[((int64_t)j * m + i) * W + 1] = ki;
+  }
+  __syncthreads();
+  // column norms
+  for (int j = warp; j < n; j += nw) {
+    double s = 0;
+    const double* col = A + (int64_t)j * m * W;
+    for (int i = lane; i < m * W; i += 32) s += col[i] * col[i];
+    s = warp_sum_d(s);
+    if (lane == 0) {
+      vn1[j] = sqrt(s);
+      vn2[j] = vn1[j];
+    }
+  }
+  for (int j = threadIdx.x; j < n; j += blockDim.x) piv[j] = j;
+  __syncthreads();
+
+  // ---- 2. column-pivoted Householder QR
+  const int kmax = min(m, n);
+  const bool fixed = a.tol >= 1.0;
+  const int rank_fixed = fixed ? min((int)a.tol, kmax) : kmax;
+  double r00 = 0.0;
+  int rank = 0;
+  const double tol3z = sqrt(2.220446049250313e-16);
+  for (int k = 0; k < kmax; ++k) {
+    // pivot: first index of the largest partial norm
+    double best = -1.0;
+    int bi = k;
+    for (int j = k + threadIdx.x; j < n; j += blockDim.x) {
+      const double v = vn1[j];
+      if (v > best) {
+        best = v;
+        bi = j;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    __syncthreads();
+    if (lane == 0) {
+      red[warp] = best;
+      reinterpret_cast<int*>(red + 32)[warp] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bb = red[0];
+      int bj = reinterpret_cast<int*>(red + 32)[0];
+      for (int w = 1; w < nw; ++w) {
+        const double ob = red[w];
+        const int oi = reinterpret_cast<int*>(red + 32)[w];
+        if (ob > bb || (ob == bb && oi < bj)) {
+          bb = ob;
+          bj = oi;
+        }
+      }
+      s_k = bj;
+    }
+    __syncthreads();
+    const int p = s_k;
+    if (p != k) {
+      double* ck = A + (int64_t)k * m * W;
+      double* cp = A + (int64_t)p * m * W;
+      for (int i = threadIdx.x; i < m * W; i += blockDim.x) {
+        const double t = ck[i];
+        ck[i] = cp[i];
+        cp[i] = t;
+      }
+      if (threadIdx.x == 0) {
+        const int t = piv[k];
+        piv[k] = piv[p];
+        piv[p] = t;
+        vn1[p] = vn1[k];
+        vn2[p] = vn2[k];
+      }
+    }
+    __syncthreads();
+    // Householder reflector for column k, rows k..m-1 (complex: LAPACK zlarfg form)
+    double* ck = A + (int64_t)k * m * W;
+    double s = 0;
+    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      s += ck[i * W] * ck[i * W];
+      if (C) s += ck[i * W + 1] * ck[i * W + 1];
+    }
+    const double xnorm2 = block_sum(s, red);
+    if (threadIdx.x == 0) {
+      const double ar = ck[k * W], ai = C ? ck[k * W + 1] : 0.0;
+      double beta, taur = 0, taui = 0, scr = 0, sci = 0;
+      if (xnorm2 == 0.0 && ai == 0.0) {
+        beta = ar;  // H = I
+        taur = 0;
+        scr = 0;
+      } else {
+        const double nrm = sqrt(ar * ar + ai * ai + xnorm2);
+        beta = ar >= 0 ? -nrm : nrm;
+        taur = (beta - ar) / beta;
+        taui = -ai / beta;
+        // scale = 1 / (alpha - beta)
+        const double dr = ar - beta, di = ai;
+        const double dd = dr * dr + di * di;
+        scr = dr / dd;
+        sci = -di / dd;
+      }
+      s_scal[0] = beta;
+      s_scal[1] = taur;
+      s_scal[2] = taui;
+      s_scal[3] = 0;
+      red[60] = scr;
+      red[61] = sci;
+    }
+    __syncthreads();
+    const double beta = s_scal[0], taur = s_scal[1], taui = s_scal[2];
+    const double scr = red[60], sci = red[61];
+    if (k == 0) r00 = fabs(beta);
+    const double rkk = fabs(beta);
+    const bool stop = fixed ? (k >= rank_fixed) : (!(rkk > a.tol * r00) || r00 == 0.0);
+    if (stop) {
+      rank = k;
+      break;
+    }
+    rank = k + 1;
+    // v = [1; x(k+1:) * scale]
+    for (int i = k + threadIdx.x; i < m; i += blockDim.x) {
+      if (i == k) {
+        vv[i * W] = 1.0;
+        if (C) vv[i * W + 1] = 0.0;
+      } else {
+        const double xr = ck[i * W], xi = C ? ck[i * W + 1] : 0.0;
+        vv[i * W] = xr * scr - xi * sci;
+        if (C) vv[i * W + 1] = xr * sci + xi * scr;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      ck[k * W] = beta;
+      if (C) ck[k * W + 1] = 0.0;
+    }
+    // trailing update: A(k:, j) -= conj(tau) v (v^H A(k:, j)), one warp per column
+    for (int j = k + 1 + warp; j < n; j += nw) {
+      double* cj = A + (int64_t)j * m * W;
+      double wr = 0, wi = 0;
+      for (int i = k + lane; i < m; i += 32) {
+        const double vr = vv[i * W], vi = C ? vv[i * W + 1] : 0.0;
+        const double ar = cj[i * W], ai = C ? cj[i * W + 1] : 0.0;
+        // conj(v) * a
+        wr += vr * ar + vi * ai;
+        if (C) wi += vr * ai - vi * ar;
+      }
+      wr = warp_sum_d(wr);
+      if (C) wi = warp_sum_d(wi);
+      // f = conj(tau) * w  (H^H applied: LAPACK zgeqp3 applies H(k)^H = I - conj(tau) v v^H)
+      const double fr = taur * wr + taui * wi;
+      const double fi = C ? (taur * wi - taui * wr) : 0.0;
+      double part = 0;
+      for (int i = k + lane; i < m; i += 32) {
+        const double vr = vv[i * W], vi = C ? vv[i * W + 1] : 0.0;
+        double ar = cj[i * W] - (vr * fr - vi * fi);
+        cj[i * W] = ar;
+        if (C) {
+          double ai = cj[i * W + 1] - (vr * fi + vi * fr);
+          cj[i * W + 1] = ai;
+          if (i > k) part += ar * ar + ai * ai;
+        } else if (i > k) {
+          part += ar * ar;
+        }
+      }
+      // partial-norm downdate (LAWN 176): every lane takes the same decision
+      __syncwarp();
+      double akj2;
+      {
+        const double ar = cj[k * W], ai = C ? cj[k * W + 1] : 0.0;
+        akj2 = ar * ar + ai * ai;
+      }
+      const double v1 = vn1[j];
+      double temp = 0.0;
+      bool recompute = false;
+      if (v1 != 0.0) {
+        temp = 1.0 - akj2 / (v1 * v1);
+        temp = temp < 0 ? 0 : temp;
+        const double ratio = v1 / vn2[j];
+        recompute = temp * ratio * ratio <= tol3z;
+      }
+      if (recompute) {
+        part = warp_sum_d(part);
+        if (lane == 0) {
+          vn1[j] = sqrt(part);
+          vn2[j] = vn1[j];
+        }
+      } else if (lane == 0 && v1 != 0.0) {
+        vn1[j] = v1 * sqrt(temp);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  // ---- 3. outputs: rank, permutation, T = R11^{-1} R12 (row-major rank x (n-rank))
+  if (threadIdx.x == 0) a.rank[b] = rank;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) a.perm[off + j] = piv[j];
+  const int nr = n - rank;
+  double* T = a.t_out + a.t_off_out[b] * W;
+  if (rank > 0 && nr > 0) {
+    // column-oriented back substitution, one warp per right-hand side
+    for (int cidx = warp; cidx < nr; cidx += nw) {
+      double* bcol = A + (int64_t)(rank + cidx) * m * W;  // R12(:, c), overwritten by t
+      for (int i = rank - 1; i >= 0; --i) {
+        const double* ci = A + (int64_t)i * m * W;
+        double tr, ti = 0;
+        {
+          const double br = bcol[i * W], bi = C ? bcol[i * W + 1] : 0.0;
+          const double rr = ci[i * W], ri = C ? ci[i * W + 1] : 0.0;
+          if (C) {
+            const double dd = rr * rr + ri * ri;
+            tr = (br * rr + bi * ri) / dd;
+            ti = (bi * rr - br * ri) / dd;
+          } else {
+            tr = br / rr;
+          }
+        }
+        __syncwarp();
+        if (lane == 0) {
+          bcol[i * W] = tr;
+          if (C) bcol[i * W + 1] = ti;
+        }
+        for (int l = lane; l < i; l += 32) {
+          const double rr = ci[l * W], ri = C ? ci[l * W + 1] : 0.0;
+          bcol[l * W] -= rr * tr - ri * ti;
+          if (C) bcol[l * W + 1] -= rr * ti + ri * tr;
+        }
+        __syncwarp();
+      }
+      for (int i = lane; i < rank; i += 32) {
+        T[((int64_t)i * nr + cidx) * W] = bcol[i * W];
+        if (C) T[((int64_t)i * nr + cidx) * W + 1] = bcol[i * W + 1];
+      }
+    }
+  }
+}
+
+template <int OP>
+static int launch_skel(SkelArgs a, int nbox, int maxn, cudaStream_t st) {
+  constexpr int W = OpTraits<OP>::kComplex ? 2 : 1;
+  const size_t smem = sizeof(double) * ((size_t)2 * maxn + (size_t)a.mrows * W + 64) + sizeof(int) * (size_t)maxn;
+  if (smem > 200 * 1024) return SKF_ERR_UNSUPPORTED;
+  if (smem > 48 * 1024) SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_skel_box<OP><<<nbox, kSkelThreads, smem, st>>>(a);
+  SKF_CUDA_TRY(cudaGetLastError());
+  return SKF_OK;
+}
+
+int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
+               const double* centers, double box_length, int nproxy, double tol, int32_t* rank, int32_t* perm,
+               const int64_t* t_off_out, void* t_out, cudaStream_t st) {
+  const int ndim = (op == SKF_LAPLACE_2D || op == SKF_HELMHOLTZ_2D) ? 2 : 3;
+  const bool geom_op = op >= SKF_LAPLACE_DOUBLE_LAYER_3D;
+  const bool cplx = op == SKF_HELMHOLTZ_2D || op == SKF_HELMHOLTZ_3D || op == SKF_HELMHOLTZ_DOUBLE_LAYER_3D ||
+                    op == SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D;
+  const int W = cplx ? 2 : 1;
+  std::vector<double> tmpl = proxy_template(ndim, geom_op, nproxy);
+  const int np = (int)(tmpl.size() / ndim);
+  const int mrows = geom_op ? 2 * np : np;
+  std::vector<int64_t> hoff(nbox + 1);
+  SKF_CUDA_TRY(cudaMemcpyAsync(hoff.data(), off, sizeof(int64_t) * (nbox + 1), cudaMemcpyDeviceToHost, st));
+  SKF_CUDA_TRY(cudaStreamSynchronize(st));
+  int maxn = 1;
+  for (int b = 0; b < nbox; ++b) maxn = std::max<int>(maxn, (int)(hoff[b + 1] - hoff[b]));
+
+  double* dtmpl = nullptr;
+  SKF_CUDA_TRY(cudaMallocAsync(&dtmpl, sizeof(double) * tmpl.size(), st));
+  SKF_CUDA_TRY(cudaMemcpyAsync(dtmpl, tmpl.data(), sizeof(double) * tmpl.size(), cudaMemcpyHostToDevice, st));
+
+  // workspace in batches of boxes bounded by ~4 GiB
+  const int64_t budget = (int64_t)4 << 30;
+  int status = SKF_OK;
+  int b0 = 0;
+  while (b0 < nbox && status == SKF_OK) {
+    std::vector<int64_t> wso;
+    int64_t acc = 0;
+    int b1 = b0;
+    while (b1 < nbox) {
+      const int64_t need = (int64_t)mrows * (hoff[b1 + 1] - hoff[b1]) * W * (int64_t)sizeof(double);
+      if (b1 > b0 && acc + need > budget) break;
+      wso.push_back(acc / (int64_t)sizeof(double));
+      acc += need;
+      ++b1;
+    }
+    double* ws = nullptr;
+    int64_t* dwso = nullptr;
+    cudaError_t e = cudaMallocAsync(&ws, std::max<int64_t>(acc, 8), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dwso, sizeof(int64_t) * wso.size(), st);
+    if (e != cudaSuccess) {
+      set_last_cuda_error(e);
+      status = SKF_ERR_OOM;
+      if (ws) cudaFreeAsync(ws, st);
+      break;
+    }
+    e = cudaMemcpyAsync(dwso, wso.data(), sizeof(int64_t) * wso.size(), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+      set_last_cuda_error(e);
+      status = SKF_ERR_CUDA;
+    }
+    SkelArgs a;
+    a.off = off;
+    a.x = x;
+    a.geom = geom;
+    a.centers = centers;
+    a.tmpl = dtmpl;
+    a.np = np;
+    a.mrows = mrows;
+    a.plen = 2.95 * box_length;
+    a.kappa = kappa;
+    a.tol = tol;
+    a.ws = ws;
+    a.ws_off = dwso;
+    a.rank = rank;
+    a.perm = perm;
+    a.t_off_out = t_off_out;
+    a.t_out = static_cast<double*>(t_out);
+    a.first_box = b0;
+    int maxn_batch = 1;
+    for (int b = b0; b < b1; ++b) maxn_batch = std::max<int>(maxn_batch, (int)(hoff[b + 1] - hoff[b]));
+    if (status == SKF_OK) {
+      switch (op) {
+#define SKF_CASE(OPID) \
+  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, st); break;
+        SKF_CASE(SKF_LAPLACE_2D)
+        SKF_CASE(SKF_LAPLACE_3D)
+        SKF_CASE(SKF_HELMHOLTZ_2D)
+        SKF_CASE(SKF_HELMHOLTZ_3D)
+        SKF_CASE(SKF_LAPLACE_DOUBLE_LAYER_3D)
+        SKF_CASE(SKF_LAPLACE_ADJOINT_DOUBLE_LAYER_3D)
+        SKF_CASE(SKF_HELMHOLTZ_DOUBLE_LAYER_3D)
+        SKF_CASE(SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D)
+#undef SKF_CASE
+        default: status = SKF_ERR_ARG;
+      }
+    }
+    cudaFreeAsync(ws, st);
+    cudaFreeAsync(dwso, st);
+    b0 = b1;
+  }
+  cudaFreeAsync(dtmpl, st);
+  if (status == SKF_OK) SKF_CUDA_TRY(cudaGetLastError());
+  (void)maxn;
+  return status;
+}
+
+}  // namespace skf

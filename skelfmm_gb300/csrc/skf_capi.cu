@@ -1,0 +1,349 @@
+// skf_capi.cu — extern "C" entry points (declared in include/skf.h): plan
+// creation from a ragged build, apply (device or host buffers), the batched
+// kernel-block seam, and status strings.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "skf_internal.cuh"
+
+namespace skf {
+
+int plan_apply_device(skf_plan* p, const double* x, double* y, bool mixed, cudaStream_t st);
+int plan_time_translations(skf_plan* p, bool mixed, int reps, cudaStream_t st, float* ms);
+int kernel_apply(int op, double kappa, int npairs, int mmax, int nmax, const int32_t* m, const int32_t* n,
+                 const double* xt, const double* xs, const double* gt, const double* gs, const double* q,
+                 const int8_t* sf, double* out, bool mixed, cudaStream_t st);
+int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
+               const double* centers, double box_length, int nproxy, double tol, int32_t* rank, int32_t* perm,
+               const int64_t* t_off_out, void* t_out, cudaStream_t st);
+
+static thread_local cudaError_t g_last_cuda = cudaSuccess;
+void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+
+static bool op_is_complex(int op) {
+  return op == SKF_HELMHOLTZ_2D || op == SKF_HELMHOLTZ_3D || op == SKF_HELMHOLTZ_DOUBLE_LAYER_3D ||
+         op == SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D;
+}
+static bool op_needs_geom(int op) { return op >= SKF_LAPLACE_DOUBLE_LAYER_3D && op <= SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D; }
+static int op_dim(int op) { return (op == SKF_LAPLACE_2D || op == SKF_HELMHOLTZ_2D) ? 2 : 3; }
+
+template <typename T>
+static int upload(skf_plan* p, T** dst, const T* src, size_t n) {
+  *dst = nullptr;
+  if (n == 0) return SKF_OK;
+  void* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, n * sizeof(T));
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    return SKF_ERR_OOM;
+  }
+  p->allocations.push_back(d);
+  p->device_bytes += (int64_t)(n * sizeof(T));
+  if (src != nullptr) {
+    e = cudaMemcpy(d, src, n * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      set_last_cuda_error(e);
+      return SKF_ERR_CUDA;
+    }
+  }
+  *dst = static_cast<T*>(d);
+  return SKF_OK;
+}
+
+static void free_plan(skf_plan* p) {
+  if (!p) return;
+  for (void* a : p->allocations) cudaFree(a);
+  delete p;
+}
+
+}  // namespace skf
+
+using namespace skf;
+
+#define SKF_TRY(expr)              \
+  do {                             \
+    int _s = (expr);               \
+    if (_s != SKF_OK) {            \
+      free_plan(p);                \
+      return _s;                   \
+    }                              \
+  } while (0)
+
+extern "C" {
+
+int skf_version(void) { return 1; }
+
+const char* skf_status_string(int32_t s) {
+  switch (s) {
+    case SKF_OK: return "ok";
+    case SKF_ERR_ARG: return "invalid argument";
+    case SKF_ERR_OOM: return "device out of memory";
+    case SKF_ERR_CUDA: return cudaGetErrorString(g_last_cuda);
+    case SKF_ERR_UNSUPPORTED: return "unsupported operator or precision";
+    case SKF_ERR_ID: return "interpolative decomposition failed (non-finite proxy matrix)";
+    case SKF_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+  }
+}
+
+int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
+  if (!d || !out) return SKF_ERR_ARG;
+  *out = nullptr;
+  if (d->op < 0 || d->op >= SKF_NUM_OPS) return SKF_ERR_ARG;
+  if (d->ndim != op_dim(d->op)) return SKF_ERR_ARG;
+  if (d->nboxes <= 0 || d->nlevels <= 0 || d->root_level < 0 || d->root_level >= d->nlevels) return SKF_ERR_ARG;
+  if (!d->box_level || !d->box_off || !d->box_rank || !d->entry_xyz || !d->entry_pslot || !d->perm_entry ||
+      !d->perm_point || !d->t_off || !d->list_off || !d->list_src || !d->list_kind)
+    return SKF_ERR_ARG;
+  if (op_needs_geom(d->op) && !d->entry_geom) return SKF_ERR_ARG;
+  const int nb = d->nboxes;
+  const int64_t E = d->box_off[nb];
+  if (E <= 0 || d->box_off[0] != 0) return SKF_ERR_ARG;
+  for (int b = 0; b < nb; ++b) {
+    const int64_t bs = d->box_off[b + 1] - d->box_off[b];
+    if (bs < 0 || d->box_rank[b] < 0 || d->box_rank[b] > bs) return SKF_ERR_ARG;
+    if (d->box_level[b] < 0 || d->box_level[b] >= d->nlevels) return SKF_ERR_ARG;
+  }
+  if (d->nperm <= 0 || d->npoints <= 0) return SKF_ERR_ARG;
+  for (int64_t i = 0; i < d->nperm; ++i) {
+    if (d->perm_entry[i] < 0 || d->perm_entry[i] >= E || d->perm_point[i] < 0 || d->perm_point[i] >= d->npoints)
+      return SKF_ERR_ARG;
+  }
+  for (int64_t e = 0; e < E; ++e)
+    if (d->entry_pslot[e] < -1 || d->entry_pslot[e] >= E) return SKF_ERR_ARG;
+  const int64_t L = d->list_off[nb];
+  if (d->list_off[0] != 0 || L < 0) return SKF_ERR_ARG;
+  for (int64_t l = 0; l < L; ++l) {
+    if (d->list_src[l] < 0 || d->list_src[l] >= nb || d->list_kind[l] < 0 || d->list_kind[l] > 3) return SKF_ERR_ARG;
+  }
+  const bool cplx = op_is_complex(d->op);
+  const int W = cplx ? 2 : 1;
+  for (int b = 0; b < nb; ++b) {
+    const int64_t bs = d->box_off[b + 1] - d->box_off[b];
+    const int64_t r = d->box_rank[b];
+    if (r > 0 && d->box_level[b] > d->root_level) {
+      if (d->t_off[b] < 0 || d->t_off[b] + r * (bs - r) > d->t_len) return SKF_ERR_ARG;
+    }
+  }
+
+  skf_plan* p = new skf_plan();
+  p->op = d->op;
+  p->ndim = d->ndim;
+  p->nboxes = nb;
+  p->nlevels = d->nlevels;
+  p->root_level = d->root_level;
+  p->cplx = cplx;
+  p->kappa = d->kappa;
+  p->E = E;
+  p->N = d->npoints;
+  p->nperm = d->nperm;
+  p->t_len = d->t_len;
+  p->nlist = L;
+
+  // entry coordinates: FP64 (x,y,z,0) and the FP32 hi/lo split
+  std::vector<double4_32a> xyz(E);
+  std::vector<float4> hi(E), lo(E);
+  for (int64_t e = 0; e < E; ++e) {
+    double c[3] = {0, 0, 0};
+    for (int k = 0; k < d->ndim; ++k) c[k] = d->entry_xyz[e * d->ndim + k];
+    xyz[e] = make_double4_32a(c[0], c[1], c[2], 0.0);
+    float h[3], l[3];
+    for (int k = 0; k < 3; ++k) {
+      h[k] = (float)c[k];
+      l[k] = (float)(c[k] - (double)h[k]);
+    }
+    hi[e] = make_float4(h[0], h[1], h[2], 0.f);
+    lo[e] = make_float4(l[0], l[1], l[2], 0.f);
+  }
+  SKF_TRY(upload(p, &p->xyz64, xyz.data(), E));
+  SKF_TRY(upload(p, &p->hi32, hi.data(), E));
+  SKF_TRY(upload(p, &p->lo32, lo.data(), E));
+  if (d->entry_geom) {
+    std::vector<double4_32a> g(E);
+    std::vector<float4> g32(E);
+    for (int64_t e = 0; e < E; ++e) {
+      g[e] = make_double4_32a(d->entry_geom[3 * e], d->entry_geom[3 * e + 1], d->entry_geom[3 * e + 2], 0.0);
+      g32[e] = make_float4((float)g[e].x, (float)g[e].y, (float)g[e].z, 0.f);
+    }
+    SKF_TRY(upload(p, &p->geom64, g.data(), E));
+    SKF_TRY(upload(p, &p->geom32, g32.data(), E));
+  }
+  SKF_TRY(upload(p, &p->box_off, d->box_off, (size_t)nb + 1));
+  SKF_TRY(upload(p, &p->box_rank, d->box_rank, (size_t)nb));
+  SKF_TRY(upload(p, &p->pslot, d->entry_pslot, (size_t)E));
+  SKF_TRY(upload(p, &p->perm_entry, d->perm_entry, (size_t)d->nperm));
+  SKF_TRY(upload(p, &p->perm_point, d->perm_point, (size_t)d->nperm));
+  SKF_TRY(upload(p, &p->t_off, d->t_off, (size_t)nb));
+  const int64_t tl = std::max<int64_t>(d->t_len, 1);
+  SKF_TRY(upload(p, &p->t64, (const double*)nullptr, (size_t)tl * W));
+  if (d->t_len > 0) {
+    cudaError_t e = cudaMemcpy(p->t64, d->t_data, sizeof(double) * d->t_len * W, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      set_last_cuda_error(e);
+      free_plan(p);
+      return SKF_ERR_CUDA;
+    }
+  }
+  {
+    std::vector<float> t32((size_t)tl * W, 0.f);
+    for (int64_t i = 0; i < d->t_len * W; ++i) t32[i] = (float)d->t_data[i];
+    SKF_TRY(upload(p, &p->t32, t32.data(), (size_t)tl * W));
+  }
+  SKF_TRY(upload(p, &p->list_off, d->list_off, (size_t)nb + 1));
+  SKF_TRY(upload(p, &p->list_src, d->list_src, (size_t)std::max<int64_t>(L, 1)));
+  SKF_TRY(upload(p, &p->list_kind, d->list_kind, (size_t)std::max<int64_t>(L, 1)));
+
+  // level box lists for the upward/downward passes
+  p->levels.assign(d->nlevels, LevelBoxes());
+  {
+    std::vector<std::vector<int32_t>> lb(d->nlevels);
+    for (int b = 0; b < nb; ++b) {
+      const int lev = d->box_level[b];
+      const int r = d->box_rank[b];
+      const int bs = (int)(d->box_off[b + 1] - d->box_off[b]);
+      if (lev > d->root_level && r > 0 && bs > 0) {
+        lb[lev].push_back(b);
+        p->levels[lev].max_red = std::max(p->levels[lev].max_red, bs - r);
+        p->levels[lev].max_rank = std::max(p->levels[lev].max_rank, r);
+      }
+    }
+    for (int lev = 0; lev < d->nlevels; ++lev) {
+      p->levels[lev].n = (int)lb[lev].size();
+      if (!lb[lev].empty()) SKF_TRY(upload(p, &p->levels[lev].dev, lb[lev].data(), lb[lev].size()));
+    }
+  }
+
+  // translation work items: (target box, row tile), most expensive first
+  {
+    int64_t pairs = 0;
+    std::vector<int64_t> src_sum(nb, 0);
+    for (int b = 0; b < nb; ++b) {
+      int64_t s = 0;
+      for (int64_t l = d->list_off[b]; l < d->list_off[b + 1]; ++l) {
+        const int sb = d->list_src[l];
+        s += d->box_off[sb + 1] - d->box_off[sb];
+      }
+      src_sum[b] = s;
+      pairs += s * (d->box_off[b + 1] - d->box_off[b]);
+    }
+    p->pairs = pairs;
+    for (int pass = 0; pass < 2; ++pass) {
+      const int tile = kTransThreads * (pass == 0 ? kRowsPerThreadF64 : kRowsPerThreadF32);
+      std::vector<std::pair<int64_t, std::pair<int32_t, int32_t>>> items;
+      for (int b = 0; b < nb; ++b) {
+        const int bs = (int)(d->box_off[b + 1] - d->box_off[b]);
+        if (bs == 0 || d->list_off[b + 1] == d->list_off[b]) continue;
+        for (int r0 = 0; r0 < bs; r0 += tile) {
+          const int64_t rows = std::min(tile, bs - r0);
+          items.push_back({rows * src_sum[b], {b, r0}});
+        }
+      }
+      std::stable_sort(items.begin(), items.end(),
+                       [](const auto& a, const auto& b) { return a.first > b.first; });
+      std::vector<int32_t> wb(items.size()), wr(items.size());
+      for (size_t i = 0; i < items.size(); ++i) {
+        wb[i] = items[i].second.first;
+        wr[i] = items[i].second.second;
+      }
+      WorkList& w = pass == 0 ? p->work64 : p->work32;
+      w.n = (int)items.size();
+      if (w.n > 0) {
+        SKF_TRY(upload(p, &w.box, wb.data(), wb.size()));
+        SKF_TRY(upload(p, &w.row, wr.data(), wr.size()));
+      }
+    }
+  }
+
+  SKF_TRY(upload(p, &p->q, (const double*)nullptr, (size_t)E * W));
+  SKF_TRY(upload(p, &p->qh, (const double*)nullptr, (size_t)E * W));
+  SKF_TRY(upload(p, &p->u, (const double*)nullptr, (size_t)E * W));
+  SKF_TRY(upload(p, &p->uh, (const double*)nullptr, (size_t)E * W));
+  cudaError_t e1 = cudaMemset(p->q, 0, sizeof(double) * E * W);
+  cudaError_t e2 = cudaMemset(p->qh, 0, sizeof(double) * E * W);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    set_last_cuda_error(e1 != cudaSuccess ? e1 : e2);
+    free_plan(p);
+    return SKF_ERR_CUDA;
+  }
+  *out = p;
+  return SKF_OK;
+}
+
+int skf_plan_destroy(skf_plan* p) {
+  free_plan(p);
+  return SKF_OK;
+}
+
+int skf_plan_query(const skf_plan* p, skf_plan_info* info) {
+  if (!p || !info) return SKF_ERR_ARG;
+  info->nentries = p->E;
+  info->npairs_fused = p->pairs;
+  info->t_scalars = p->t_len;
+  info->device_bytes = p->device_bytes;
+  info->nwork = p->work32.n;
+  info->is_complex = p->cplx ? 1 : 0;
+  return SKF_OK;
+}
+
+int skf_plan_apply(skf_plan* p, const void* x, void* y, int32_t precision, void* stream) {
+  if (!p || !x || !y) return SKF_ERR_ARG;
+  if (precision != SKF_PREC_FP64 && precision != SKF_PREC_MIXED) return SKF_ERR_ARG;
+  return plan_apply_device(p, static_cast<const double*>(x), static_cast<double*>(y), precision == SKF_PREC_MIXED,
+                           static_cast<cudaStream_t>(stream));
+}
+
+int skf_plan_apply_host(skf_plan* p, const void* xh, void* yh, int32_t precision, void* stream) {
+  if (!p || !xh || !yh) return SKF_ERR_ARG;
+  if (precision != SKF_PREC_FP64 && precision != SKF_PREC_MIXED) return SKF_ERR_ARG;
+  const int W = p->cplx ? 2 : 1;
+  const size_t bytes = sizeof(double) * (size_t)p->N * W;
+  if (!p->xbuf) {
+    if (upload(p, &p->xbuf, (const double*)nullptr, (size_t)p->N * W) != SKF_OK) return SKF_ERR_OOM;
+    if (upload(p, &p->ybuf, (const double*)nullptr, (size_t)p->N * W) != SKF_OK) return SKF_ERR_OOM;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SKF_CUDA_TRY(cudaMemcpyAsync(p->xbuf, xh, bytes, cudaMemcpyHostToDevice, st));
+  int s = plan_apply_device(p, p->xbuf, p->ybuf, precision == SKF_PREC_MIXED, st);
+  if (s != SKF_OK) return s;
+  SKF_CUDA_TRY(cudaMemcpyAsync(yh, p->ybuf, bytes, cudaMemcpyDeviceToHost, st));
+  SKF_CUDA_TRY(cudaStreamSynchronize(st));
+  return SKF_OK;
+}
+
+int skf_plan_time_translations(skf_plan* p, int32_t precision, int32_t reps, void* stream, float* ms_out) {
+  if (!p || !ms_out || reps <= 0) return SKF_ERR_ARG;
+  return plan_time_translations(p, precision == SKF_PREC_MIXED, reps, static_cast<cudaStream_t>(stream), ms_out);
+}
+
+int skf_kernel_apply(int32_t op, double kappa, int32_t npairs, int32_t mmax, int32_t nmax, const int32_t* m,
+                     const int32_t* n, const double* xt, const double* xs, const double* gt, const double* gs,
+                     const void* q, const int8_t* self_flag, void* out, int32_t precision, void* stream) {
+  if (op < 0 || op >= SKF_NUM_OPS || npairs < 0 || mmax < 0 || nmax < 0) return SKF_ERR_ARG;
+  if (npairs == 0 || mmax == 0) return SKF_OK;
+  if (!m || !n || !xt || !xs || !q || !out) return SKF_ERR_ARG;
+  if (op_needs_geom(op) && ((op == SKF_LAPLACE_DOUBLE_LAYER_3D || op == SKF_HELMHOLTZ_DOUBLE_LAYER_3D) ? !gs : !gt))
+    return SKF_ERR_ARG;
+  if (precision != SKF_PREC_FP64 && precision != SKF_PREC_MIXED) return SKF_ERR_ARG;
+  return kernel_apply(op, kappa, npairs, mmax, nmax, m, n, xt, xs, gt, gs, static_cast<const double*>(q), self_flag,
+                      static_cast<double*>(out), precision == SKF_PREC_MIXED, static_cast<cudaStream_t>(stream));
+}
+
+int skf_skel_boxes(int32_t op, double kappa, int32_t nbox, const int64_t* off, const double* x, const double* geom,
+                   const double* centers, double box_length, int32_t nproxy, double tol, int32_t* rank, int32_t* perm,
+                   const int64_t* t_off_out, void* t_out, void* stream) {
+  if (op < 0 || op >= SKF_NUM_OPS || nbox < 0 || nproxy <= 0 || !(box_length > 0) || !(tol > 0)) return SKF_ERR_ARG;
+  if (nbox == 0) return SKF_OK;
+  if (!off || !x || !centers || !rank || !perm || !t_off_out || !t_out) return SKF_ERR_ARG;
+  if (op_needs_geom(op) && !geom) return SKF_ERR_ARG;
+  return skel_boxes(op, kappa, nbox, off, x, geom, centers, box_length, nproxy, tol, rank, perm, t_off_out, t_out,
+                    static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

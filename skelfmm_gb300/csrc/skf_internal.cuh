@@ -1,0 +1,87 @@
+// skf_internal.cuh — plan layout and helpers shared by the CUDA sources.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/skf.h"
+
+#define SKF_CUDA_TRY(expr)                 \
+  do {                                     \
+    cudaError_t _e = (expr);               \
+    if (_e != cudaSuccess) {               \
+      skf::set_last_cuda_error(_e);        \
+      return SKF_ERR_CUDA;                 \
+    }                                      \
+  } while (0)
+
+namespace skf {
+
+void set_last_cuda_error(cudaError_t e);
+
+// Translation kernel geometry: 128 threads per block; rows per thread depend
+// on the precision (FP64: 1, mixed: 2).
+constexpr int kTransThreads = 128;
+constexpr int kRowsPerThreadF64 = 1;
+constexpr int kRowsPerThreadF32 = 2;
+constexpr int kTileSrcF64 = 64;
+constexpr int kTileSrcF32 = 128;
+
+struct LevelBoxes {
+  int32_t* dev = nullptr;  // box ids at this level with rank > 0
+  int n = 0;
+  int max_red = 0;   // max (bs - rank)
+  int max_rank = 0;  // max rank
+};
+
+struct WorkList {
+  int32_t* box = nullptr;
+  int32_t* row = nullptr;
+  int n = 0;
+};
+
+}  // namespace skf
+
+// HBM layout of a built operator.  Entries of box b occupy
+// [box_off[b], box_off[b+1]) in every per-entry array.
+struct skf_plan {
+  int op = 0, ndim = 3, nboxes = 0, nlevels = 0, root_level = 0;
+  bool cplx = false;
+  double kappa = 0.0;
+  int64_t E = 0, N = 0, nperm = 0, t_len = 0, nlist = 0;
+  int64_t pairs = 0;  // kernel evaluations per apply
+
+  // per box
+  int64_t* box_off = nullptr;
+  int32_t* box_rank = nullptr;
+  // per entry
+  double4_32a* xyz64 = nullptr;   // (x, y, z, 0)
+  double4_32a* geom64 = nullptr;  // (nx, ny, nz, 0) or null
+  float4* hi32 = nullptr;     // fl32(x)
+  float4* lo32 = nullptr;     // fl32(x - fl32(x))
+  float4* geom32 = nullptr;
+  int64_t* pslot = nullptr;
+  // leaf permutation
+  int64_t* perm_entry = nullptr;
+  int64_t* perm_point = nullptr;
+  // T blocks
+  int64_t* t_off = nullptr;
+  double* t64 = nullptr;
+  float* t32 = nullptr;
+  // interaction lists
+  int64_t* list_off = nullptr;
+  int32_t* list_src = nullptr;
+  int8_t* list_kind = nullptr;
+  skf::WorkList work64, work32;
+  std::vector<skf::LevelBoxes> levels;  // indexed by level
+  // apply vectors (scalars; complex: 2 doubles per entry)
+  double* q = nullptr;
+  double* qh = nullptr;
+  double* u = nullptr;
+  double* uh = nullptr;
+  double* xbuf = nullptr;  // staging for apply_host
+  double* ybuf = nullptr;
+  int64_t device_bytes = 0;
+  std::vector<void*> allocations;
+};

@@ -1,0 +1,229 @@
+"""Device plan of a built skeletonization (ragged CSR layout) and its apply.
+
+``RaggedBuild`` is the host-side description the C ABI consumes
+(``skf_plan_desc`` in ``include/skf.h``); ``Plan`` owns the device copy.
+``ragged_from_reference`` converts a build in the reference's padded layout
+(``RecursiveSkeletonization`` after ``setup_lists``,
+skelfmm/recursive_skel.py:106-120, 515-539, 622-780) — the data
+``SkelFMMBatched.build_from_copy`` (skelfmm/batched_fmm.py:92-174) copies to
+the device — into that description.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .operators import cuda_op_id, is_complex_op
+
+
+@dataclass
+class RaggedBuild:
+    op: int
+    ndim: int
+    kappa: float
+    npoints: int
+    nlevels: int
+    root_level: int
+    box_level: np.ndarray   # int32 [nb]
+    box_off: np.ndarray     # int64 [nb+1]
+    box_rank: np.ndarray    # int32 [nb]
+    entry_xyz: np.ndarray   # f64 [E, ndim]
+    entry_geom: np.ndarray | None  # f64 [E, 3]
+    entry_pslot: np.ndarray  # int64 [E]
+    perm_entry: np.ndarray   # int64 [N]
+    perm_point: np.ndarray   # int64 [N]
+    t_off: np.ndarray        # int64 [nb]
+    t_data: np.ndarray       # f64 or c128, flat
+    list_off: np.ndarray     # int64 [nb+1]
+    list_src: np.ndarray     # int32 [L]
+    list_kind: np.ndarray    # int8 [L]
+
+    @property
+    def nboxes(self):
+        return int(self.box_level.shape[0])
+
+    @property
+    def nentries(self):
+        return int(self.box_off[-1])
+
+
+def lists_to_csr(nboxes, pairs_by_kind):
+    """Group (target, source) pair arrays of each kind by target box."""
+    tgt, src, kind = [], [], []
+    for k, pairs in pairs_by_kind:
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        tgt.append(pairs[:, 0])
+        src.append(pairs[:, 1])
+        kind.append(np.full(pairs.shape[0], k, dtype=np.int8))
+    tgt = np.concatenate(tgt) if tgt else np.zeros(0, np.int64)
+    src = np.concatenate(src) if src else np.zeros(0, np.int64)
+    kind = np.concatenate(kind) if kind else np.zeros(0, np.int8)
+    order = np.argsort(tgt, kind="stable")
+    counts = np.bincount(tgt, minlength=nboxes)
+    off = np.zeros(nboxes + 1, dtype=np.int64)
+    np.cumsum(counts, out=off[1:])
+    return off, src[order].astype(np.int32), kind[order].astype(np.int8)
+
+
+def ragged_from_reference(tree, fmm, operator, kappa=0.0):
+    """Ragged description of a build held in the reference's padded layout.
+
+    ``fmm`` exposes the attributes of a reference ``RecursiveSkeletonization``
+    after ``setup_lists`` (a live object, or a mapping of the same arrays).
+    """
+    get = (lambda k: fmm[k]) if isinstance(fmm, dict) else (lambda k: getattr(fmm, k))
+    nb = tree.nboxes
+    bs = np.asarray(get("bs_list"), dtype=np.int64)
+    rk = np.asarray(get("rank_list"), dtype=np.int64)
+    XX = np.asarray(get("XX_list"))
+    max_bs = XX.shape[1]
+    min_rank = int(get("min_rank"))
+    root_level = int(get("root_level"))
+    levels = tree.get_boxes_levels().astype(np.int32)
+    off = np.zeros(nb + 1, dtype=np.int64)
+    np.cumsum(bs, out=off[1:])
+    E = int(off[-1])
+    # padded index box*max_bs + k  ->  entry index off[box] + k
+    def pad_to_entry(p):
+        p = np.asarray(p, dtype=np.int64)
+        return off[p // max_bs] + p % max_bs
+
+    mask = np.arange(max_bs)[None, :] < bs[:, None]
+    entry_xyz = XX[mask]
+    entry_geom = None
+    geom_list = None
+    try:
+        geom_list = get("geom_list")
+    except (KeyError, AttributeError):
+        geom_list = None
+    if geom_list is not None:
+        entry_geom = np.asarray(geom_list)[mask]
+    pslot = np.full(E, -1, dtype=np.int64)
+    pslot[pad_to_entry(get("child_skel_inds"))] = pad_to_entry(get("box_skel_inds"))
+    perm_entry = pad_to_entry(get("short_vec_inds"))
+    perm_point = np.asarray(get("long_vec_inds"), dtype=np.int64)
+
+    cplx = is_complex_op(operator)
+    proj = np.asarray(get("proj_list"))
+    projt = np.asarray(get("proj_list_tree"))
+    tree_boxes = np.asarray(get("tree_boxes"), dtype=np.int64)
+    leaf = tree.are_leaves(np.arange(nb))
+    t_off = np.full(nb, -1, dtype=np.int64)
+    blocks = []
+    acc = 0
+    for b in range(nb):
+        r, s = int(rk[b]), int(bs[b])
+        if r <= 0 or levels[b] <= root_level:
+            continue
+        if leaf[b]:
+            T = proj[b, :r, r - min_rank: s - min_rank]
+        else:
+            T = projt[int(np.searchsorted(tree_boxes, b)), :r, r - min_rank: s - min_rank]
+        t_off[b] = acc
+        blocks.append(np.ascontiguousarray(T).ravel())
+        acc += r * (s - r)
+    dt = np.complex128 if cplx else np.float64
+    t_data = np.concatenate(blocks).astype(dt) if blocks else np.zeros(1, dt)
+
+    coll = np.vstack((np.asarray(get("leaf_uskel_from_qskel_list")).reshape(-1, 2),
+                      np.asarray(get("tree_uskel_from_qskel_list")).reshape(-1, 2)))
+    list_off, list_src, list_kind = lists_to_csr(nb, [
+        (_lib.KIND_COLLEAGUE, coll),
+        (_lib.KIND_COARSE_UP, get("uskel_from_q_list")),
+        (_lib.KIND_COARSE_DOWN, get("u_from_qskel_list")),
+        (_lib.KIND_ROOT, get("u_from_q_list")),
+    ])
+    return RaggedBuild(
+        op=cuda_op_id(operator), ndim=tree.ndim, kappa=float(kappa), npoints=int(tree.N),
+        nlevels=int(tree.nlevels), root_level=root_level, box_level=levels, box_off=off,
+        box_rank=rk.astype(np.int32), entry_xyz=np.ascontiguousarray(entry_xyz, dtype=np.float64),
+        entry_geom=None if entry_geom is None else np.ascontiguousarray(entry_geom, dtype=np.float64),
+        entry_pslot=pslot, perm_entry=perm_entry, perm_point=perm_point, t_off=t_off,
+        t_data=t_data, list_off=list_off, list_src=list_src, list_kind=list_kind,
+    )
+
+
+class Plan:
+    """A built operator resident on the device (owns an ``skf_plan``)."""
+
+    def __init__(self, rb: RaggedBuild):
+        lib = _lib.load()
+        self.rb = rb
+        self.op = rb.op
+        self.npoints = rb.npoints
+        self.is_complex = is_complex_op(rb.op)
+        keep = {}
+
+        def arr(name, a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep[name] = a
+            return a.ctypes.data
+
+        d = _lib.PlanDesc()
+        d.op = rb.op
+        d.ndim = rb.ndim
+        d.kappa = rb.kappa
+        d.npoints = rb.npoints
+        d.nboxes = rb.nboxes
+        d.nlevels = rb.nlevels
+        d.root_level = rb.root_level
+        d.box_level = arr("box_level", rb.box_level, np.int32)
+        d.box_off = arr("box_off", rb.box_off, np.int64)
+        d.box_rank = arr("box_rank", rb.box_rank, np.int32)
+        d.entry_xyz = arr("entry_xyz", rb.entry_xyz, np.float64)
+        d.entry_geom = None if rb.entry_geom is None else arr("entry_geom", rb.entry_geom, np.float64)
+        d.entry_pslot = arr("entry_pslot", rb.entry_pslot, np.int64)
+        d.nperm = int(rb.perm_entry.shape[0])
+        d.perm_entry = arr("perm_entry", rb.perm_entry, np.int64)
+        d.perm_point = arr("perm_point", rb.perm_point, np.int64)
+        d.t_off = arr("t_off", rb.t_off, np.int64)
+        tdt = np.complex128 if self.is_complex else np.float64
+        d.t_data = arr("t_data", rb.t_data, tdt)
+        d.t_len = int(rb.t_data.shape[0])
+        d.list_off = arr("list_off", rb.list_off, np.int64)
+        d.list_src = arr("list_src", rb.list_src, np.int32)
+        d.list_kind = arr("list_kind", rb.list_kind, np.int8)
+        h = ctypes.c_void_p()
+        _lib.check(lib.skf_plan_create(ctypes.byref(d), ctypes.byref(h)), "skf_plan_create")
+        self._h = h
+        info = _lib.PlanInfo()
+        _lib.check(lib.skf_plan_query(h, ctypes.byref(info)), "skf_plan_query")
+        self.info = info
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().skf_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def apply_device(self, x, y, precision=_lib.PREC_FP64, stream=None):
+        """y = A x for device tensors (float64 / complex128, length N)."""
+        _lib.check(_lib.load().skf_plan_apply(self._h, _lib.ptr(x), _lib.ptr(y), int(precision),
+                                              None if stream is None else ctypes.c_void_p(stream)),
+                   "skf_plan_apply")
+
+    def apply_host(self, x, y, precision=_lib.PREC_FP64, stream=None):
+        """y = A x for host arrays; copies in and out, synchronises."""
+        _lib.check(_lib.load().skf_plan_apply_host(self._h, _lib.ptr(x), _lib.ptr(y), int(precision),
+                                                   None if stream is None else ctypes.c_void_p(stream)),
+                   "skf_plan_apply_host")
+
+    def time_translations(self, precision, reps=5, stream=None):
+        ms = ctypes.c_float()
+        _lib.check(_lib.load().skf_plan_time_translations(self._h, int(precision), int(reps),
+                                                          None if stream is None else ctypes.c_void_p(stream),
+                                                          ctypes.byref(ms)), "skf_plan_time_translations")
+        return float(ms.value)

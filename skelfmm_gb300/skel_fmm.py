@@ -1,0 +1,248 @@
+"""Public fast-apply object (drop-in for ``skelfmm.SkelFMM``, skelfmm/skel_fmm.py:55-282).
+
+Same constructor arguments, ``build()``, ``apply(x)``, ``matvec``,
+``relerr_fmm_apply_check`` and ``benchmark_matvec``.  The build runs the
+proxy IDs on the GPU; the apply runs entirely on the GPU:
+
+* ``use_single_precision=False`` (default) -> the plain FP64 apply;
+* ``use_single_precision=True`` -> the mixed apply (FP32 kernel evaluation
+  with FP64 accumulation, FP32 interpolation matrices).
+
+``precision="fp64"|"mixed"`` selects the same explicitly.
+"""
+
+from __future__ import annotations
+
+import contextlib
+import io
+from time import perf_counter
+
+import numpy as np
+import torch
+
+from . import _lib
+from .operators import _require_operator, cuda_op_id, is_complex_op
+from .plan import Plan
+from .recursive_skel import RecursiveSkeletonization
+from .tree import BalancedTree
+
+
+def warmup_cuda_fmm_apply(apply, x):
+    """Run one apply so later timings exclude first-call costs (skel_fmm.py:38-52)."""
+    device = getattr(apply, "device", None)
+    if not (isinstance(device, torch.device) and device.type == "cuda"):
+        return False
+    apply.apply(x)
+    torch.cuda.synchronize(device)
+    return True
+
+
+class SkelFMM:
+    """Build and apply a fast operator on one GPU."""
+
+    def __init__(self, points, operator, geometry=None, tol=1e-5, rank_or_tol=None, leaf_size=200,
+                 use_single_precision=False, param=0.0, quiet=True, keep_host_fmm=False, defer_build=False,
+                 npoints_max=500, p="auto", max_bs=-1, max_rank=-1, precision=None):
+        self.points = np.asarray(points, dtype=np.float64)
+        self.operator = _require_operator(operator)
+        self.geometry = geometry
+        self.param = param
+        self.rank_or_tol = tol if rank_or_tol is None else rank_or_tol
+        self.leaf_size = leaf_size
+        self.tree = None
+        self.nlevels = 0
+        self.nboxes = 0
+        self.nleaves = 0
+        self._quiet = quiet
+        self._keep_host_fmm = keep_host_fmm
+        self._use_single_precision = use_single_precision
+        if precision is None:
+            precision = "mixed" if use_single_precision else "fp64"
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
+        self._build_npoints_max = npoints_max
+        self._build_p = p
+        self._max_bs_limit = max_bs
+        self._max_rank_limit = max_rank
+        self._is_built = False
+        self._lazy_build_notice_printed = False
+
+        self.fmm = None
+        self.plan = None
+        self.batched = None
+        self.device = torch.device("cuda") if torch.cuda.is_available() else None
+        self.kernel_backend = "cuda-sm103a"
+        self.tree_time_seconds = 0.0
+        self.skel_time_seconds = 0.0
+        self.setup_time_seconds = 0.0
+        self.build_time_seconds = 0.0
+        self.rank_max = 0
+        self.host_build_storage_bytes = 0
+        self.host_storage_bytes = 0
+        self.device_storage_bytes = 0
+        self.total_storage_bytes = 0
+        self.nbytes = 0
+        if not defer_build:
+            self.build()
+
+    @property
+    def _prec_code(self):
+        return _lib.PREC_MIXED if self.precision == "mixed" else _lib.PREC_FP64
+
+    def _synchronize(self):
+        if isinstance(self.device, torch.device) and self.device.type == "cuda":
+            torch.cuda.synchronize(self.device)
+
+    def build(self, *, npoints_max=None, p=None, verbose=False):
+        if self._is_built:
+            return self
+        if self.device is None:
+            raise RuntimeError("SkelFMM needs a CUDA device (there is no CPU path)")
+        cuda_op_id(self.operator)  # rejects operators without a CUDA kernel
+        if npoints_max is None:
+            npoints_max = self._build_npoints_max
+        t_build = perf_counter()
+        ctx = contextlib.ExitStack()
+        with ctx as stack:
+            if self._quiet:
+                stack.enter_context(contextlib.redirect_stdout(io.StringIO()))
+                stack.enter_context(contextlib.redirect_stderr(io.StringIO()))
+            t0 = perf_counter()
+            self.tree = BalancedTree(self.points, leaf_size=self.leaf_size)
+            self.tree_time_seconds = perf_counter() - t0
+            self.nlevels = self.tree.nlevels
+            self.nboxes = self.tree.nboxes
+            self.nleaves = self.tree.nleaves
+            fmm = RecursiveSkeletonization(self.tree, self.operator, kappa=self.param, tol=self.rank_or_tol,
+                                           max_bs=self._max_bs_limit, max_rank=self._max_rank_limit,
+                                           geometry=self.geometry, device=self.device)
+            t0 = perf_counter()
+            fmm.skel_tree(npoints_max=npoints_max, verbose=verbose)
+            self.skel_time_seconds = perf_counter() - t0
+            t0 = perf_counter()
+            fmm.setup_lists(verbose=verbose)
+            self.plan = Plan(fmm.ragged())
+            torch.cuda.synchronize(self.device)
+            self.setup_time_seconds = perf_counter() - t0
+        self.build_time_seconds = perf_counter() - t_build
+        self.rank_max = fmm.rank_max
+        self.fmm = fmm if self._keep_host_fmm else None
+        self.device_storage_bytes = int(self.plan.info.device_bytes)
+        self.host_build_storage_bytes = int(sum(p.nbytes for p in fmm.pid if p is not None))
+        self.host_storage_bytes = self.host_build_storage_bytes if self._keep_host_fmm else 0
+        self.total_storage_bytes = self.host_storage_bytes + self.device_storage_bytes
+        self.nbytes = self.total_storage_bytes
+        self._is_built = True
+        return self
+
+    def _ensure_built(self, *, announce=False):
+        if getattr(self, "_is_built", True):
+            return
+        if announce and not self._lazy_build_notice_printed:
+            print("\tBuilding SkelFMM on first matvec; subsequent matvecs will be fast.")
+            self._lazy_build_notice_printed = True
+        self.build()
+
+    def apply(self, x):
+        self._ensure_built(announce=True)
+        x_np = np.asarray(x)
+        if x_np.ndim != 1:
+            raise ValueError("apply expects a 1D vector")
+        if x_np.shape[0] != self.points.shape[0]:
+            raise ValueError("Source vector length must match the number of points")
+        cplx = is_complex_op(self.operator)
+        if np.iscomplexobj(x_np) and not cplx:
+            re = self.apply(np.ascontiguousarray(x_np.real))
+            im = self.apply(np.ascontiguousarray(x_np.imag))
+            return re + 1j * im
+        dt = np.complex128 if cplx else np.float64
+        xin = np.ascontiguousarray(x_np, dtype=dt)
+        y = np.empty_like(xin)
+        self.plan.apply_host(xin, y, self._prec_code)
+        if not cplx and self._use_single_precision:
+            return y.astype(np.float32)
+        if cplx and self._use_single_precision:
+            return y.astype(np.complex64)
+        return y
+
+    def matvec(self, x):
+        return self.apply(x)
+
+    def apply_device(self, x, y=None):
+        """y = A x for CUDA tensors (no host copies)."""
+        self._ensure_built()
+        cplx = is_complex_op(self.operator)
+        dt = torch.complex128 if cplx else torch.float64
+        x = x.to(dtype=dt).contiguous()
+        if y is None:
+            y = torch.empty_like(x)
+        self.plan.apply_device(x, y, self._prec_code, torch.cuda.current_stream(x.device).cuda_stream)
+        return y
+
+    def direct_apply(self, x, indices):
+        """FP64 direct sum ``(K x)[indices]`` on the GPU (kernel evaluated on the fly)."""
+        from .kernels import batched_kernel_apply
+
+        idx = np.asarray(indices, dtype=np.int64)
+        cplx = is_complex_op(self.operator)
+        dev = self.device
+        src = torch.from_numpy(self.points).to(dev).unsqueeze(0)
+        xq = torch.from_numpy(np.ascontiguousarray(x, dtype=np.complex128 if cplx else np.float64)).to(dev)
+        gs = gt = None
+        if self.operator.geometry_side == "source":
+            gs = torch.from_numpy(np.ascontiguousarray(self.geometry, dtype=np.float64)).to(dev).unsqueeze(0)
+        out = []
+        for s in range(0, idx.shape[0], 4096):
+            t = idx[s: s + 4096]
+            trg = torch.from_numpy(np.ascontiguousarray(self.points[t])).to(dev).unsqueeze(0)
+            gtt = None
+            if self.operator.geometry_side == "target":
+                gtt = torch.from_numpy(np.ascontiguousarray(self.geometry[t], dtype=np.float64)).to(dev).unsqueeze(0)
+            # a coincident pair contributes 0, as in the dense kernels
+            out.append(batched_kernel_apply(cuda_op_id(self.operator), xq.unsqueeze(0).unsqueeze(-1), trg, src,
+                                            param=self.param, geom_trg=gtt if gtt is not None else gt,
+                                            geom_src=gs)[0, :, 0].cpu().numpy())
+        return np.concatenate(out)
+
+    def relerr_fmm_apply_check(self, x, *, ncheck=64, seed=0, indices=None):
+        """||y_dense - y_fmm||_inf / ||y_dense||_inf on a subset of targets (skel_fmm.py:218-257).
+
+        The dense reference is an FP64 direct sum evaluated on the GPU.
+        """
+        self._ensure_built()
+        x = np.asarray(x)
+        if x.ndim != 1:
+            raise ValueError("relerr_fmm_apply_check expects a 1D source vector")
+        if x.shape[0] != self.points.shape[0]:
+            raise ValueError("Source vector length must match the number of points")
+        if indices is None:
+            rng = np.random.default_rng(seed)
+            indices = rng.choice(self.points.shape[0], size=min(int(ncheck), self.points.shape[0]), replace=False)
+        else:
+            indices = np.asarray(indices, dtype=int)
+        y_fast = self.apply(x)
+        y_true = self.direct_apply(x, indices)
+        denom = max(np.linalg.norm(y_true, ord=np.inf), 1e-30)
+        return np.linalg.norm(y_true - y_fast[indices], ord=np.inf) / denom
+
+    def benchmark_matvec(self, *, nrepeat=3, warmup=1, seed=0):
+        self._ensure_built()
+        x = np.random.RandomState(seed).randn(self.points.shape[0])
+        warmup_cuda_fmm_apply(self, x)
+        for _ in range(max(warmup, 0)):
+            self.apply(x)
+            self._synchronize()
+        times = []
+        for _ in range(max(nrepeat, 1)):
+            self._synchronize()
+            t0 = perf_counter()
+            self.apply(x)
+            self._synchronize()
+            times.append(perf_counter() - t0)
+        return {
+            "times_seconds": tuple(times),
+            "avg_seconds": float(np.mean(times)),
+            "min_seconds": float(np.min(times)),
+            "max_seconds": float(np.max(times)),
+        }

@@ -106,6 +106,7 @@ def make_builds():
         )
         if geometry is not None:
             out["geometry"] = geometry
+            out["geom_list"] = fmm.geom_list
         if y_serial is not None:
             out["y_serial"] = y_serial
         np.savez_compressed(os.path.join(HERE, f"build_{name}.npz"), **out)
