@@ -46,7 +46,8 @@ extern "C" {
 
 /* apply precision */
 #define SKF_PREC_FP64 0  /* everything in FP64 */
-#define SKF_PREC_MIXED 1 /* FP32 kernel evaluation (FP64 tile sums), FP32 T/T^T */
+#define SKF_PREC_MIXED 1     /* FP32 kernel evaluation (compensated FP32 sums), FP64 T/T^T */
+#define SKF_PREC_MIXED_T32 2 /* as SKF_PREC_MIXED with FP32 T/T^T (half the T bytes) */
 
 /* translation kinds in a target box's interaction list */
 #define SKF_KIND_COLLEAGUE 0   /* u += K q ; uskel[:r_u] -= K[:r_u,:r_s] qskel[:r_s] */
@@ -109,6 +110,12 @@ int skf_plan_apply(skf_plan* plan, const void* x, void* y, int32_t precision, vo
 /* Same product with HOST buffers: copies x in, applies, copies y out, and
    synchronises the stream before returning. */
 int skf_plan_apply_host(skf_plan* plan, const void* x_host, void* y_host, int32_t precision, void* stream);
+
+/* Plan options.  SKF_OPT_SCALAR_MIXED: 1 = run the mixed translations with the
+   scalar FP32 kernel even where the packed FP32x2 kernel exists (Laplace), 0 =
+   default.  Used to cross-check the two kernels. */
+#define SKF_OPT_SCALAR_MIXED 1
+int skf_plan_set_option(skf_plan* plan, int32_t option, int64_t value);
 
 /* Time the plan's translation kernel alone (device time in ms over `reps`
    launches, measured with events on `stream`).  For roofline reporting. */

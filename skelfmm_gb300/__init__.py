@@ -1,6 +1,27 @@
-"""GB300-native strong-recursive-skeletonization FMM (drop-in for skelfmm)."""
+"""GB300-native strong-recursive-skeletonization FMM (drop-in for skelfmm).
+
+Public surface mirrors ``skelfmm/__init__.py``: ``SkelFMM``,
+``RecursiveSkeletonization``, ``operators`` and ``warmup_cuda_fmm_apply``;
+``Plan`` is the device-resident apply (the role of ``SkelFMMBatched``).
+"""
 
 from . import operators  # noqa: F401
 from .tree import BalancedTree  # noqa: F401
 
-__all__ = ["operators", "BalancedTree"]
+__all__ = ["SkelFMM", "RecursiveSkeletonization", "Plan", "operators", "warmup_cuda_fmm_apply", "BalancedTree"]
+
+
+def __getattr__(name):
+    if name in ("SkelFMM", "warmup_cuda_fmm_apply"):
+        from . import skel_fmm
+
+        return getattr(skel_fmm, name)
+    if name == "RecursiveSkeletonization":
+        from .recursive_skel import RecursiveSkeletonization
+
+        return RecursiveSkeletonization
+    if name in ("Plan", "SkelFMMBatched"):
+        from .plan import Plan
+
+        return Plan
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")

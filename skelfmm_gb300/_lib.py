@@ -23,6 +23,7 @@ SKF_ERR_TIMEOUT = 6
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_MIXED_T32 = 2
 
 KIND_COLLEAGUE = 0
 KIND_COARSE_UP = 1
@@ -63,6 +64,7 @@ SIGNATURES = {
     "skf_plan_query": (_i32, [_p, ctypes.POINTER(PlanInfo)]),
     "skf_plan_apply": (_i32, [_p, _p, _p, _i32, _p]),
     "skf_plan_apply_host": (_i32, [_p, _p, _p, _i32, _p]),
+    "skf_plan_set_option": (_i32, [_p, _i32, _i64]),
     "skf_plan_time_translations": (_i32, [_p, _i32, _i32, _p, ctypes.POINTER(ctypes.c_float)]),
     "skf_kernel_apply": (_i32, [_i32, _f64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p, _p, _p, _p, _i32, _p]),
     "skf_skel_boxes": (_i32, [_i32, _f64, _i32, _p, _p, _p, _p, _f64, _i32, _f64, _p, _p, _p, _p, _p]),

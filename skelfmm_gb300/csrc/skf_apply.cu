@@ -25,6 +25,7 @@
 
 #include "skf_internal.cuh"
 #include "skf_kernels.cuh"
+#include "skf_translate.cuh"
 
 namespace skf {
 
@@ -52,6 +53,20 @@ __global__ void k_permute_out(const int64_t* __restrict__ pe, const int64_t* __r
     } else {
       y[p] = u[e];
     }
+  }
+}
+
+// FP32 effective charges for the mixed translations (see skf_plan::q32):
+// rounded once from the FP64 vectors, with q - qskel formed in FP64.
+__global__ void k_charges32(int64_t n, int W, const int32_t* __restrict__ skel, const double* __restrict__ q,
+                            const double* __restrict__ qh, float* __restrict__ q32, float* __restrict__ qhn32,
+                            float* __restrict__ qd32) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const bool sk = skel[i / W] != 0;
+    const double v = q[i];
+    q32[i] = (float)v;
+    qhn32[i] = sk ? (float)(-qh[i]) : 0.f;
+    qd32[i] = sk ? (float)(v - qh[i]) : (float)v;
   }
 }
 
@@ -187,325 +202,6 @@ __global__ void __launch_bounds__(256) k_down(const int32_t* __restrict__ boxes,
   }
 }
 
-// ------------------------------------------------------------------ translations
-struct TransArgs {
-  const int32_t* work_box;
-  const int32_t* work_row;
-  const int64_t* box_off;
-  const int32_t* box_rank;
-  const int64_t* list_off;
-  const int32_t* list_src;
-  const int8_t* list_kind;
-  const double4_32a* xyz64;
-  const double4_32a* geom64;
-  const float4* hi32;
-  const float4* lo32;
-  const float4* geom32;
-  const double* q;
-  const double* qh;
-  double* u;
-  double* uh;
-  double kappa;
-};
-
-// Effective source charges of entry j of source box s for a translation kind:
-// acc_u += K * c1 ; acc_h += K * c2 (acc_h only kept for the target's skeleton rows).
-__device__ __forceinline__ void kind_charges(int kind, int j, int rs, double q, double qh, double& c1, double& c2) {
-  const bool sk = j < rs;
-  switch (kind) {
-    case SKF_KIND_COLLEAGUE:
-      c1 = q;
-      c2 = sk ? -qh : 0.0;
-      break;
-    case SKF_KIND_COARSE_UP:
-      c1 = q;
-      c2 = -q;
-      break;
-    case SKF_KIND_COARSE_DOWN:
-      c1 = sk ? q - qh : q;
-      c2 = 0.0;
-      break;
-    default:
-      c1 = q;
-      c2 = 0.0;
-      break;
-  }
-}
-
-// FP64 translation kernel: one block per (target box, 128-row tile).
-template <int OP>
-__global__ void __launch_bounds__(kTransThreads) k_translate_f64(TransArgs a) {
-  constexpr bool C = OpTraits<OP>::kComplex;
-  constexpr int G = OpTraits<OP>::kGeom;
-  constexpr int TS = kTileSrcF64;
-  __shared__ double2 sA[TS];  // x, y
-  __shared__ double2 sB[TS];  // z, c1r
-  __shared__ double2 sC[TS];  // c2r, c1i
-  __shared__ double2 sD[TS];  // c2i, gx
-  __shared__ double2 sE[TS];  // gy, gz
-
-  const int U = a.work_box[blockIdx.x];
-  const int row0 = a.work_row[blockIdx.x];
-  const int64_t offU = a.box_off[U];
-  const int bsU = (int)(a.box_off[U + 1] - offU);
-  const int rU = a.box_rank[U];
-  const int row = row0 + threadIdx.x;
-  const bool valid = row < bsU;
-  const int64_t eT = offU + (valid ? row : bsU - 1);
-  const double4_32a tp = a.xyz64[eT];
-  double4_32a tg = make_double4_32a(0, 0, 0, 0);
-  if (G == 2) tg = a.geom64[eT];
-  const bool need_h = (row0 + (threadIdx.x & ~31)) < rU;
-
-  double aur = 0, aui = 0, ahr = 0, ahi = 0;
-  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
-  for (int64_t l = l0; l < l1; ++l) {
-    const int s = a.list_src[l];
-    const int kind = a.list_kind[l];
-    const int64_t offS = a.box_off[s];
-    const int bsS = (int)(a.box_off[s + 1] - offS);
-    const int rS = a.box_rank[s];
-    const int nh = (kind == SKF_KIND_COLLEAGUE) ? rS : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
-    for (int t0 = 0; t0 < bsS; t0 += TS) {
-      const int nt = min(TS, bsS - t0);
-      __syncthreads();
-      for (int j = threadIdx.x; j < nt; j += blockDim.x) {
-        const int js = t0 + j;
-        const int64_t e = offS + js;
-        const double4_32a p = a.xyz64[e];
-        double c1r, c2r, c1i = 0, c2i = 0;
-        if (C) {
-          kind_charges(kind, js, rS, a.q[2 * e], a.qh[2 * e], c1r, c2r);
-          kind_charges(kind, js, rS, a.q[2 * e + 1], a.qh[2 * e + 1], c1i, c2i);
-        } else {
-          kind_charges(kind, js, rS, a.q[e], a.qh[e], c1r, c2r);
-        }
-        sA[j] = make_double2(p.x, p.y);
-        sB[j] = make_double2(p.z, c1r);
-        sC[j] = make_double2(c2r, c1i);
-        double4_32a g = make_double4_32a(0, 0, 0, 0);
-        if (G == 1) g = a.geom64[e];
-        sD[j] = make_double2(c2i, g.x);
-        sE[j] = make_double2(g.y, g.z);
-      }
-      __syncthreads();
-      const bool doh = need_h && (t0 < nh);
-      for (int j = 0; j < nt; ++j) {
-        const double2 A = sA[j], B = sB[j];
-        const double dx = tp.x - A.x, dy = tp.y - A.y, dz = tp.z - B.x;
-        double gx = 0, gy = 0, gz = 0;
-        if (G == 1) {
-          gx = sD[j].y;
-          const double2 E = sE[j];
-          gy = E.x;
-          gz = E.y;
-        } else if (G == 2) {
-          gx = tg.x;
-          gy = tg.y;
-          gz = tg.z;
-        }
-        double kr, ki;
-        eval_f64<OP>(dx, dy, dz, gx, gy, gz, a.kappa, kr, ki);
-        const double2 Cc = sC[j];
-        if (C) {
-          const double c1i = Cc.y;
-          aur = fma(kr, B.y, fma(-ki, c1i, aur));
-          aui = fma(kr, c1i, fma(ki, B.y, aui));
-          if (doh) {
-            const double c2i = sD[j].x;
-            ahr = fma(kr, Cc.x, fma(-ki, c2i, ahr));
-            ahi = fma(kr, c2i, fma(ki, Cc.x, ahi));
-          }
-        } else {
-          aur = fma(kr, B.y, aur);
-          if (doh) ahr = fma(kr, Cc.x, ahr);
-        }
-      }
-    }
-  }
-  if (valid) {
-    const bool sk = row < rU;
-    if (C) {
-      a.u[2 * eT] = aur;
-      a.u[2 * eT + 1] = aui;
-      a.uh[2 * eT] = sk ? ahr : 0.0;
-      a.uh[2 * eT + 1] = sk ? ahi : 0.0;
-    } else {
-      a.u[eT] = aur;
-      a.uh[eT] = sk ? ahr : 0.0;
-    }
-  }
-}
-
-// Mixed translation kernel: FP32 kernel evaluation with accurate, level-
-// independent differences (hi/lo split coordinates), FP32 partial sums per
-// source tile, FP64 accumulation across tiles.  Two target rows per thread.
-template <int OP>
-__global__ void __launch_bounds__(kTransThreads) k_translate_f32(TransArgs a) {
-  constexpr bool C = OpTraits<OP>::kComplex;
-  constexpr int G = OpTraits<OP>::kGeom;
-  constexpr int TS = kTileSrcF32;
-  constexpr int RPT = kRowsPerThreadF32;
-  __shared__ float4 sA[TS];  // hx, hy, hz, c1r
-  __shared__ float4 sB[TS];  // lx, ly, lz, c2r
-  __shared__ float4 sC[(C || G == 1) ? TS : 1];  // c1i, c2i, gx, gy
-  __shared__ float sD[(G == 1) ? TS : 1];        // gz
-
-  const int U = a.work_box[blockIdx.x];
-  const int row0 = a.work_row[blockIdx.x];
-  const int64_t offU = a.box_off[U];
-  const int bsU = (int)(a.box_off[U + 1] - offU);
-  const int rU = a.box_rank[U];
-  const float kappa = (float)a.kappa;
-
-  float4 th[RPT], tl[RPT], tg[RPT];
-  int64_t eT[RPT];
-  bool valid[RPT];
-#pragma unroll
-  for (int k = 0; k < RPT; ++k) {
-    const int row = row0 + threadIdx.x + k * kTransThreads;
-    valid[k] = row < bsU;
-    eT[k] = offU + (valid[k] ? row : bsU - 1);
-    th[k] = a.hi32[eT[k]];
-    tl[k] = a.lo32[eT[k]];
-    tg[k] = (G == 2) ? a.geom32[eT[k]] : make_float4(0, 0, 0, 0);
-  }
-  const bool need_h = (row0 + (threadIdx.x & ~31)) < rU;
-
-  double aur[RPT], aui[RPT], ahr[RPT], ahi[RPT];
-#pragma unroll
-  for (int k = 0; k < RPT; ++k) aur[k] = aui[k] = ahr[k] = ahi[k] = 0.0;
-
-  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
-  for (int64_t l = l0; l < l1; ++l) {
-    const int s = a.list_src[l];
-    const int kind = a.list_kind[l];
-    const int64_t offS = a.box_off[s];
-    const int bsS = (int)(a.box_off[s + 1] - offS);
-    const int rS = a.box_rank[s];
-    const int nh = (kind == SKF_KIND_COLLEAGUE) ? rS : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
-    for (int t0 = 0; t0 < bsS; t0 += TS) {
-      const int nt = min(TS, bsS - t0);
-      __syncthreads();
-      for (int j = threadIdx.x; j < nt; j += blockDim.x) {
-        const int js = t0 + j;
-        const int64_t e = offS + js;
-        const float4 h = a.hi32[e], lo = a.lo32[e];
-        double c1r, c2r, c1i = 0, c2i = 0;
-        if (C) {
-          kind_charges(kind, js, rS, a.q[2 * e], a.qh[2 * e], c1r, c2r);
-          kind_charges(kind, js, rS, a.q[2 * e + 1], a.qh[2 * e + 1], c1i, c2i);
-        } else {
-          kind_charges(kind, js, rS, a.q[e], a.qh[e], c1r, c2r);
-        }
-        sA[j] = make_float4(h.x, h.y, h.z, (float)c1r);
-        sB[j] = make_float4(lo.x, lo.y, lo.z, (float)c2r);
-        if (C || G == 1) {
-          float4 g = (G == 1) ? a.geom32[e] : make_float4(0, 0, 0, 0);
-          sC[j] = make_float4((float)c1i, (float)c2i, g.x, g.y);
-          if (G == 1) sD[j] = g.z;
-        }
-      }
-      __syncthreads();
-      const bool doh = need_h && (t0 < nh);
-      float pur[RPT], pui[RPT], phr[RPT], phi[RPT];
-#pragma unroll
-      for (int k = 0; k < RPT; ++k) pur[k] = pui[k] = phr[k] = phi[k] = 0.f;
-      if (doh) {
-#pragma unroll 2
-        for (int j = 0; j < nt; ++j) {
-          const float4 A = sA[j], B = sB[j];
-          float4 Cc = make_float4(0, 0, 0, 0);
-          if (C || G == 1) Cc = sC[j];
-#pragma unroll
-          for (int k = 0; k < RPT; ++k) {
-            const float dx = (th[k].x - A.x) + (tl[k].x - B.x);
-            const float dy = (th[k].y - A.y) + (tl[k].y - B.y);
-            const float dz = (th[k].z - A.z) + (tl[k].z - B.z);
-            float gx = 0, gy = 0, gz = 0;
-            if (G == 1) {
-              gx = Cc.z;
-              gy = Cc.w;
-              gz = sD[j];
-            } else if (G == 2) {
-              gx = tg[k].x;
-              gy = tg[k].y;
-              gz = tg[k].z;
-            }
-            float kr, ki;
-            eval_f32<OP>(dx, dy, dz, gx, gy, gz, kappa, kr, ki);
-            if (C) {
-              pur[k] = fmaf(kr, A.w, fmaf(-ki, Cc.x, pur[k]));
-              pui[k] = fmaf(kr, Cc.x, fmaf(ki, A.w, pui[k]));
-              phr[k] = fmaf(kr, B.w, fmaf(-ki, Cc.y, phr[k]));
-              phi[k] = fmaf(kr, Cc.y, fmaf(ki, B.w, phi[k]));
-            } else {
-              pur[k] = fmaf(kr, A.w, pur[k]);
-              phr[k] = fmaf(kr, B.w, phr[k]);
-            }
-          }
-        }
-      } else {
-#pragma unroll 2
-        for (int j = 0; j < nt; ++j) {
-          const float4 A = sA[j], B = sB[j];
-          float4 Cc = make_float4(0, 0, 0, 0);
-          if (C || G == 1) Cc = sC[j];
-#pragma unroll
-          for (int k = 0; k < RPT; ++k) {
-            const float dx = (th[k].x - A.x) + (tl[k].x - B.x);
-            const float dy = (th[k].y - A.y) + (tl[k].y - B.y);
-            const float dz = (th[k].z - A.z) + (tl[k].z - B.z);
-            float gx = 0, gy = 0, gz = 0;
-            if (G == 1) {
-              gx = Cc.z;
-              gy = Cc.w;
-              gz = sD[j];
-            } else if (G == 2) {
-              gx = tg[k].x;
-              gy = tg[k].y;
-              gz = tg[k].z;
-            }
-            float kr, ki;
-            eval_f32<OP>(dx, dy, dz, gx, gy, gz, kappa, kr, ki);
-            if (C) {
-              pur[k] = fmaf(kr, A.w, fmaf(-ki, Cc.x, pur[k]));
-              pui[k] = fmaf(kr, Cc.x, fmaf(ki, A.w, pui[k]));
-            } else {
-              pur[k] = fmaf(kr, A.w, pur[k]);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < RPT; ++k) {
-        aur[k] += (double)pur[k];
-        ahr[k] += (double)phr[k];
-        if (C) {
-          aui[k] += (double)pui[k];
-          ahi[k] += (double)phi[k];
-        }
-      }
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < RPT; ++k) {
-    if (!valid[k]) continue;
-    const int row = row0 + threadIdx.x + k * kTransThreads;
-    const bool sk = row < rU;
-    const int64_t e = eT[k];
-    if (C) {
-      a.u[2 * e] = aur[k];
-      a.u[2 * e + 1] = aui[k];
-      a.uh[2 * e] = sk ? ahr[k] : 0.0;
-      a.uh[2 * e + 1] = sk ? ahi[k] : 0.0;
-    } else {
-      a.u[e] = aur[k];
-      a.uh[e] = sk ? ahr[k] : 0.0;
-    }
-  }
-}
-
 // ------------------------------------------------------------------ dispatch
 template <int OP>
 static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
@@ -526,9 +222,33 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
   a.uh = p->uh;
   a.kappa = p->kappa;
   if (mixed) {
-    a.work_box = p->work32.box;
-    a.work_row = p->work32.row;
-    if (p->work32.n > 0) k_translate_f32<OP><<<p->work32.n, kTransThreads, 0, st>>>(a);
+    TransArgs32 b;
+    b.work_box = p->work32.box;
+    b.work_row = p->work32.row;
+    b.box_off = p->box_off;
+    b.box_rank = p->box_rank;
+    b.list_off = p->list_off;
+    b.list_src = p->list_src;
+    b.list_kind = p->list_kind;
+    b.hi32 = p->hi32;
+    b.lo32 = p->lo32;
+    b.geom32 = p->geom32;
+    b.q32 = p->q32;
+    b.qhn32 = p->qhn32;
+    b.qd32 = p->qd32;
+    b.u = p->u;
+    b.uh = p->uh;
+    b.kappa = (float)p->kappa;
+    static_assert(32 * kX2Rows == kT32Threads * kRowsPerThreadF32, "work tiles are shared by both mixed kernels");
+    if (p->work32.n > 0) {
+      if constexpr (OP == SKF_LAPLACE_2D || OP == SKF_LAPLACE_3D) {
+        if (!p->scalar_mixed) {
+          k_translate_f32x2<OP><<<p->work32.n, 32, 0, st>>>(b);
+          return;
+        }
+      }
+      k_translate_f32<OP><<<p->work32.n, kT32Threads, 0, st>>>(b);
+    }
   } else {
     a.work_box = p->work64.box;
     a.work_row = p->work64.row;
@@ -557,8 +277,12 @@ static int grid_for(int64_t n, int threads) {
   return (int)g;
 }
 
-int plan_apply_device(skf_plan* p, const double* x, double* y, bool mixed, cudaStream_t st) {
+// precision: SKF_PREC_FP64, SKF_PREC_MIXED (FP32 kernel evaluation, FP64 T),
+// SKF_PREC_MIXED_T32 (FP32 kernel evaluation, FP32 T).
+int plan_apply_device(skf_plan* p, const double* x, double* y, int precision, cudaStream_t st) {
   const int W = p->cplx ? 2 : 1;
+  const bool mixed = precision != SKF_PREC_FP64;
+  const bool t32 = precision == SKF_PREC_MIXED_T32;
   SKF_CUDA_TRY(cudaMemsetAsync(p->u, 0, sizeof(double) * p->E * W, st));
   SKF_CUDA_TRY(cudaMemsetAsync(p->uh, 0, sizeof(double) * p->E * W, st));
   const int g = grid_for(p->nperm, 256);
@@ -570,12 +294,16 @@ int plan_apply_device(skf_plan* p, const double* x, double* y, bool mixed, cudaS
     if (L.n == 0) continue;
     const size_t sm = sizeof(double) * (size_t)std::max(L.max_red, 1) * W;
     if (p->cplx) {
-      if (mixed) k_up<true, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->q, p->qh);
+      if (t32) k_up<true, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->q, p->qh);
       else k_up<true, double><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t64, p->pslot, p->q, p->qh);
     } else {
-      if (mixed) k_up<false, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->q, p->qh);
+      if (t32) k_up<false, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->q, p->qh);
       else k_up<false, double><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t64, p->pslot, p->q, p->qh);
     }
+  }
+  if (mixed) {
+    const int gc = grid_for(p->E * W, 256);
+    k_charges32<<<gc, 256, 0, st>>>(p->E * W, W, p->entry_skel, p->q, p->qh, p->q32, p->qhn32, p->qd32);
   }
   translate_dispatch(p, mixed, st);
   // downward
@@ -584,10 +312,10 @@ int plan_apply_device(skf_plan* p, const double* x, double* y, bool mixed, cudaS
     if (L.n == 0) continue;
     const size_t sm = sizeof(double) * (size_t)std::max(L.max_rank, 1) * W;
     if (p->cplx) {
-      if (mixed) k_down<true, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->u, p->uh);
+      if (t32) k_down<true, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->u, p->uh);
       else k_down<true, double><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t64, p->pslot, p->u, p->uh);
     } else {
-      if (mixed) k_down<false, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->u, p->uh);
+      if (t32) k_down<false, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->u, p->uh);
       else k_down<false, double><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t64, p->pslot, p->u, p->uh);
     }
   }

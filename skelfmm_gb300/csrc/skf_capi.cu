@@ -15,7 +15,7 @@
 
 namespace skf {
 
-int plan_apply_device(skf_plan* p, const double* x, double* y, bool mixed, cudaStream_t st);
+int plan_apply_device(skf_plan* p, const double* x, double* y, int precision, cudaStream_t st);
 int plan_time_translations(skf_plan* p, bool mixed, int reps, cudaStream_t st, float* ms);
 int kernel_apply(int op, double kappa, int npairs, int mmax, int nmax, const int32_t* m, const int32_t* n,
                  const double* xt, const double* xs, const double* gt, const double* gs, const double* q,
@@ -235,7 +235,7 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
     }
     p->pairs = pairs;
     for (int pass = 0; pass < 2; ++pass) {
-      const int tile = kTransThreads * (pass == 0 ? kRowsPerThreadF64 : kRowsPerThreadF32);
+      const int tile = pass == 0 ? kTransThreads * kRowsPerThreadF64 : kT32Threads * kRowsPerThreadF32;
       std::vector<std::pair<int64_t, std::pair<int32_t, int32_t>>> items;
       for (int b = 0; b < nb; ++b) {
         const int bs = (int)(d->box_off[b + 1] - d->box_off[b]);
@@ -265,6 +265,16 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   SKF_TRY(upload(p, &p->qh, (const double*)nullptr, (size_t)E * W));
   SKF_TRY(upload(p, &p->u, (const double*)nullptr, (size_t)E * W));
   SKF_TRY(upload(p, &p->uh, (const double*)nullptr, (size_t)E * W));
+  SKF_TRY(upload(p, &p->q32, (const float*)nullptr, (size_t)E * W));
+  SKF_TRY(upload(p, &p->qhn32, (const float*)nullptr, (size_t)E * W));
+  SKF_TRY(upload(p, &p->qd32, (const float*)nullptr, (size_t)E * W));
+  {
+    // entry -> rank of its box, needed by the FP32 charge conversion
+    std::vector<int32_t> er(E);
+    for (int b = 0; b < nb; ++b)
+      for (int64_t e = d->box_off[b]; e < d->box_off[b + 1]; ++e) er[e] = (int32_t)(e - d->box_off[b]) < d->box_rank[b] ? 1 : 0;
+    SKF_TRY(upload(p, &p->entry_skel, er.data(), (size_t)E));
+  }
   cudaError_t e1 = cudaMemset(p->q, 0, sizeof(double) * E * W);
   cudaError_t e2 = cudaMemset(p->qh, 0, sizeof(double) * E * W);
   if (e1 != cudaSuccess || e2 != cudaSuccess) {
@@ -294,14 +304,14 @@ int skf_plan_query(const skf_plan* p, skf_plan_info* info) {
 
 int skf_plan_apply(skf_plan* p, const void* x, void* y, int32_t precision, void* stream) {
   if (!p || !x || !y) return SKF_ERR_ARG;
-  if (precision != SKF_PREC_FP64 && precision != SKF_PREC_MIXED) return SKF_ERR_ARG;
-  return plan_apply_device(p, static_cast<const double*>(x), static_cast<double*>(y), precision == SKF_PREC_MIXED,
+  if (precision < SKF_PREC_FP64 || precision > SKF_PREC_MIXED_T32) return SKF_ERR_ARG;
+  return plan_apply_device(p, static_cast<const double*>(x), static_cast<double*>(y), precision,
                            static_cast<cudaStream_t>(stream));
 }
 
 int skf_plan_apply_host(skf_plan* p, const void* xh, void* yh, int32_t precision, void* stream) {
   if (!p || !xh || !yh) return SKF_ERR_ARG;
-  if (precision != SKF_PREC_FP64 && precision != SKF_PREC_MIXED) return SKF_ERR_ARG;
+  if (precision < SKF_PREC_FP64 || precision > SKF_PREC_MIXED_T32) return SKF_ERR_ARG;
   const int W = p->cplx ? 2 : 1;
   const size_t bytes = sizeof(double) * (size_t)p->N * W;
   if (!p->xbuf) {
@@ -310,16 +320,24 @@ int skf_plan_apply_host(skf_plan* p, const void* xh, void* yh, int32_t precision
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   SKF_CUDA_TRY(cudaMemcpyAsync(p->xbuf, xh, bytes, cudaMemcpyHostToDevice, st));
-  int s = plan_apply_device(p, p->xbuf, p->ybuf, precision == SKF_PREC_MIXED, st);
+  int s = plan_apply_device(p, p->xbuf, p->ybuf, precision, st);
   if (s != SKF_OK) return s;
   SKF_CUDA_TRY(cudaMemcpyAsync(yh, p->ybuf, bytes, cudaMemcpyDeviceToHost, st));
   SKF_CUDA_TRY(cudaStreamSynchronize(st));
   return SKF_OK;
 }
 
+int skf_plan_set_option(skf_plan* p, int32_t option, int64_t value) {
+  if (!p) return SKF_ERR_ARG;
+  switch (option) {
+    case SKF_OPT_SCALAR_MIXED: p->scalar_mixed = value != 0; return SKF_OK;
+    default: return SKF_ERR_ARG;
+  }
+}
+
 int skf_plan_time_translations(skf_plan* p, int32_t precision, int32_t reps, void* stream, float* ms_out) {
   if (!p || !ms_out || reps <= 0) return SKF_ERR_ARG;
-  return plan_time_translations(p, precision == SKF_PREC_MIXED, reps, static_cast<cudaStream_t>(stream), ms_out);
+  return plan_time_translations(p, precision != SKF_PREC_FP64, reps, static_cast<cudaStream_t>(stream), ms_out);
 }
 
 int skf_kernel_apply(int32_t op, double kappa, int32_t npairs, int32_t mmax, int32_t nmax, const int32_t* m,

@@ -22,9 +22,10 @@ void set_last_cuda_error(cudaError_t e);
 
 // Translation kernel geometry: 128 threads per block; rows per thread depend
 // on the precision (FP64: 1, mixed: 2).
-constexpr int kTransThreads = 128;
+constexpr int kTransThreads = 128;  // FP64 translation block
 constexpr int kRowsPerThreadF64 = 1;
-constexpr int kRowsPerThreadF32 = 2;
+constexpr int kT32Threads = 64;     // mixed translation block
+constexpr int kRowsPerThreadF32 = 4;
 constexpr int kTileSrcF64 = 64;
 constexpr int kTileSrcF32 = 128;
 
@@ -48,6 +49,7 @@ struct WorkList {
 struct skf_plan {
   int op = 0, ndim = 3, nboxes = 0, nlevels = 0, root_level = 0;
   bool cplx = false;
+  bool scalar_mixed = false;  // force the scalar FP32 translation kernel (comparison/testing)
   double kappa = 0.0;
   int64_t E = 0, N = 0, nperm = 0, t_len = 0, nlist = 0;
   int64_t pairs = 0;  // kernel evaluations per apply
@@ -78,6 +80,13 @@ struct skf_plan {
   // apply vectors (scalars; complex: 2 doubles per entry)
   double* q = nullptr;
   double* qh = nullptr;
+  // FP32 effective charges for the mixed translations (written after the
+  // upward pass): q32 = q; qhn32 = -qskel on skeleton entries, else 0;
+  // qd32 = q - qskel on skeleton entries, else q.
+  float* q32 = nullptr;
+  float* qhn32 = nullptr;
+  float* qd32 = nullptr;
+  int32_t* entry_skel = nullptr;  // 1 if the entry is in its box's skeleton
   double* u = nullptr;
   double* uh = nullptr;
   double* xbuf = nullptr;  // staging for apply_host

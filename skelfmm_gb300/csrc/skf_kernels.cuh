@@ -75,11 +75,12 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // ---------------------------------------------------------------- evaluation
 // d = x_target - y_source; gs/gt = source/target normals (3D geometry kernels).
 // Output: kr (real part) and ki (imag part, complex kernels only).
-template <int OP>
+// MASK: test r == 0 (needed only where coincident points can meet).
+template <int OP, bool MASK = true>
 __device__ __forceinline__ void eval_f64(double dx, double dy, double dz, double gx, double gy,
                                          double gz, double kappa, double& kr, double& ki) {
   const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
-  if (!(r2 > 0.0)) {
+  if (MASK && !(r2 > 0.0)) {
     kr = 0.0;
     ki = 0.0;
     return;
@@ -128,21 +129,21 @@ __device__ __forceinline__ void eval_f64(double dx, double dy, double dz, double
 
 // FP32 evaluation from an accurate difference vector (see the translation
 // kernel: differences are formed from hi/lo split coordinates).
-template <int OP>
+template <int OP, bool MASK = true>
 __device__ __forceinline__ void eval_f32(float dx, float dy, float dz, float gx, float gy,
                                          float gz, float kappa, float& kr, float& ki) {
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   if constexpr (OP == SKF_LAPLACE_2D) {
     // log r = (ln 2 / 2) * log2(r^2)
     const float v = 0.34657359027997264f * lg2_approx(r2);
-    kr = (r2 > 0.f) ? v : 0.f;
+    kr = (!MASK || r2 > 0.f) ? v : 0.f;
     ki = 0.f;
   } else if constexpr (OP == SKF_LAPLACE_3D) {
     const float v = rsqrt_approx(r2);
-    kr = (r2 > 0.f) ? v : 0.f;
+    kr = (!MASK || r2 > 0.f) ? v : 0.f;
     ki = 0.f;
   } else if constexpr (OP == SKF_HELMHOLTZ_2D) {
-    if (r2 > 0.f) {
+    if (!MASK || r2 > 0.f) {
       const float r = sqrtf(r2);
       kr = j0f(kappa * r);
       ki = y0f(kappa * r);
@@ -151,7 +152,7 @@ __device__ __forceinline__ void eval_f32(float dx, float dy, float dz, float gx,
       ki = 0.f;
     }
   } else if constexpr (OP == SKF_HELMHOLTZ_3D) {
-    if (r2 > 0.f) {
+    if (!MASK || r2 > 0.f) {
       const float ir = rsqrt_approx(r2);
       const float r = r2 * ir;
       float s, c;
@@ -163,7 +164,7 @@ __device__ __forceinline__ void eval_f32(float dx, float dy, float dz, float gx,
       ki = 0.f;
     }
   } else {
-    if (r2 > 0.f) {
+    if (!MASK || r2 > 0.f) {
       const float ir = rsqrt_approx(r2);
       const float ir3 = ir * ir * ir;
       const float rotn = dx * gx + dy * gy + dz * gz;

@@ -1,0 +1,558 @@
+// skf_translate.cuh — the translation kernels (near field + skeleton
+// translations of every level in one launch).
+//
+// One thread block owns a tile of target rows of one box U and walks U's
+// interaction list (colleagues incl. U itself, coarse-up, coarse-down, root);
+// for every source box it stages the sources in shared memory and
+// accumulates, per target row,
+//   u  += sum_j K(x_i, y_j) c1_j           (all rows)
+//   uh += sum_j K(x_i, y_j) c2_j           (U's skeleton rows)
+// with the effective charges c1/c2 of the translation kind (kind_charges).
+// No atomics: a row is written by exactly one block, so applies are bitwise
+// reproducible.  Coincident points only meet in U's self pair (identical
+// points share a box at every level), so only self pairs test r == 0.
+#pragma once
+#include "skf_internal.cuh"
+#include "skf_kernels.cuh"
+
+namespace skf {
+
+struct TransArgs {
+  const int32_t* work_box;
+  const int32_t* work_row;
+  const int64_t* box_off;
+  const int32_t* box_rank;
+  const int64_t* list_off;
+  const int32_t* list_src;
+  const int8_t* list_kind;
+  const double4_32a* xyz64;
+  const double4_32a* geom64;
+  const float4* hi32;
+  const float4* lo32;
+  const float4* geom32;
+  const double* q;
+  const double* qh;
+  double* u;
+  double* uh;
+  double kappa;
+};
+
+// Effective source charges of entry j of source box s for a translation kind:
+// acc_u += K * c1 ; acc_h += K * c2.
+__device__ __forceinline__ void kind_charges(int kind, int j, int rs, double q, double qh, double& c1, double& c2) {
+  const bool sk = j < rs;
+  switch (kind) {
+    case SKF_KIND_COLLEAGUE:
+      c1 = q;
+      c2 = sk ? -qh : 0.0;
+      break;
+    case SKF_KIND_COARSE_UP:
+      c1 = q;
+      c2 = -q;
+      break;
+    case SKF_KIND_COARSE_DOWN:
+      c1 = sk ? q - qh : q;
+      c2 = 0.0;
+      break;
+    default:
+      c1 = q;
+      c2 = 0.0;
+      break;
+  }
+}
+
+// ------------------------------------------------------------------ FP64
+template <int OP>
+__global__ void __launch_bounds__(kTransThreads) k_translate_f64(TransArgs a) {
+  constexpr bool C = OpTraits<OP>::kComplex;
+  constexpr int G = OpTraits<OP>::kGeom;
+  constexpr int TS = kTileSrcF64;
+  __shared__ double2 sA[TS];  // x, y
+  __shared__ double2 sB[TS];  // z, c1r
+  __shared__ double2 sC[TS];  // c2r, c1i
+  __shared__ double2 sD[TS];  // c2i, gx
+  __shared__ double2 sE[TS];  // gy, gz
+
+  const int U = a.work_box[blockIdx.x];
+  const int row0 = a.work_row[blockIdx.x];
+  const int64_t offU = a.box_off[U];
+  const int bsU = (int)(a.box_off[U + 1] - offU);
+  const int rU = a.box_rank[U];
+  const int row = row0 + threadIdx.x;
+  const bool valid = row < bsU;
+  const int64_t eT = offU + (valid ? row : bsU - 1);
+  const double4_32a tp = a.xyz64[eT];
+  double4_32a tg = make_double4_32a(0, 0, 0, 0);
+  if (G == 2) tg = a.geom64[eT];
+  const bool need_h = (row0 + (threadIdx.x & ~31)) < rU;
+
+  double aur = 0, aui = 0, ahr = 0, ahi = 0;
+  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
+  for (int64_t l = l0; l < l1; ++l) {
+    const int s = a.list_src[l];
+    const int kind = a.list_kind[l];
+    const int64_t offS = a.box_off[s];
+    const int bsS = (int)(a.box_off[s + 1] - offS);
+    const int rS = a.box_rank[s];
+    const int nh = (kind == SKF_KIND_COLLEAGUE) ? rS : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
+    const bool self = (s == U);
+    for (int t0 = 0; t0 < bsS; t0 += TS) {
+      const int nt = min(TS, bsS - t0);
+      __syncthreads();
+      for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        const int js = t0 + j;
+        const int64_t e = offS + js;
+        const double4_32a p = a.xyz64[e];
+        double c1r, c2r, c1i = 0, c2i = 0;
+        if (C) {
+          kind_charges(kind, js, rS, a.q[2 * e], a.qh[2 * e], c1r, c2r);
+          kind_charges(kind, js, rS, a.q[2 * e + 1], a.qh[2 * e + 1], c1i, c2i);
+        } else {
+          kind_charges(kind, js, rS, a.q[e], a.qh[e], c1r, c2r);
+        }
+        sA[j] = make_double2(p.x, p.y);
+        sB[j] = make_double2(p.z, c1r);
+        sC[j] = make_double2(c2r, c1i);
+        double4_32a g = make_double4_32a(0, 0, 0, 0);
+        if (G == 1) g = a.geom64[e];
+        sD[j] = make_double2(c2i, g.x);
+        sE[j] = make_double2(g.y, g.z);
+      }
+      __syncthreads();
+      const bool doh = need_h && (t0 < nh);
+      for (int j = 0; j < nt; ++j) {
+        const double2 A = sA[j], B = sB[j];
+        const double dx = tp.x - A.x, dy = tp.y - A.y, dz = tp.z - B.x;
+        double gx = 0, gy = 0, gz = 0;
+        if (G == 1) {
+          gx = sD[j].y;
+          const double2 E = sE[j];
+          gy = E.x;
+          gz = E.y;
+        } else if (G == 2) {
+          gx = tg.x;
+          gy = tg.y;
+          gz = tg.z;
+        }
+        double kr, ki;
+        if (self) {
+          eval_f64<OP>(dx, dy, dz, gx, gy, gz, a.kappa, kr, ki);
+        } else {
+          eval_f64<OP, false>(dx, dy, dz, gx, gy, gz, a.kappa, kr, ki);
+        }
+        const double2 Cc = sC[j];
+        if (C) {
+          const double c1i = Cc.y;
+          aur = fma(kr, B.y, fma(-ki, c1i, aur));
+          aui = fma(kr, c1i, fma(ki, B.y, aui));
+          if (doh) {
+            const double c2i = sD[j].x;
+            ahr = fma(kr, Cc.x, fma(-ki, c2i, ahr));
+            ahi = fma(kr, c2i, fma(ki, Cc.x, ahi));
+          }
+        } else {
+          aur = fma(kr, B.y, aur);
+          if (doh) ahr = fma(kr, Cc.x, ahr);
+        }
+      }
+    }
+  }
+  if (valid) {
+    const bool sk = row < rU;
+    if (C) {
+      a.u[2 * eT] = aur;
+      a.u[2 * eT + 1] = aui;
+      a.uh[2 * eT] = sk ? ahr : 0.0;
+      a.uh[2 * eT + 1] = sk ? ahi : 0.0;
+    } else {
+      a.u[eT] = aur;
+      a.uh[eT] = sk ? ahr : 0.0;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ mixed (FP32)
+// FP32 kernel evaluation.  Differences are formed from hi/lo split
+// coordinates, d = (hi_i - hi_j) + (lo_i - lo_j), which is accurate to FP32
+// rounding of d itself and identical for a pair at every level (so the add at
+// a parent level and the subtract at the child level cancel exactly).  Each
+// thread owns kRowsPerThreadF32 consecutive rows, so one broadcast
+// shared-memory read of a source feeds that many kernel evaluations.  Tile
+// sums are FP32 and are accumulated with Knuth's TwoSum (a compensated FP32
+// pair), which keeps the FP64 pipe out of the loop.
+template <int OP, bool H, bool SELF, int RPT>
+__device__ __forceinline__ void t32_tile(const float4* __restrict__ sA, const float4* __restrict__ sB,
+                                         const float4* __restrict__ sC, const float* __restrict__ sD, int nt,
+                                         const float4 (&th)[RPT], const float4 (&tl)[RPT], const float4 (&tg)[RPT],
+                                         float kappa, float (&pur)[RPT], float (&pui)[RPT], float (&phr)[RPT],
+                                         float (&phi)[RPT]) {
+  constexpr bool C = OpTraits<OP>::kComplex;
+  constexpr int G = OpTraits<OP>::kGeom;
+#pragma unroll 4
+  for (int j = 0; j < nt; ++j) {
+    const float4 A = sA[j], B = sB[j];
+    float4 Cc = make_float4(0, 0, 0, 0);
+    if (C || G == 1) Cc = sC[j];
+    float gzs = 0;
+    if (G == 1) gzs = sD[j];
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const float dx = (th[k].x - A.x) + (tl[k].x - B.x);
+      const float dy = (th[k].y - A.y) + (tl[k].y - B.y);
+      const float dz = (th[k].z - A.z) + (tl[k].z - B.z);
+      float gx = 0, gy = 0, gz = 0;
+      if (G == 1) {
+        gx = Cc.z;
+        gy = Cc.w;
+        gz = gzs;
+      } else if (G == 2) {
+        gx = tg[k].x;
+        gy = tg[k].y;
+        gz = tg[k].z;
+      }
+      float kr, ki;
+      eval_f32<OP, SELF>(dx, dy, dz, gx, gy, gz, kappa, kr, ki);
+      if (C) {
+        pur[k] = fmaf(kr, A.w, fmaf(-ki, Cc.x, pur[k]));
+        pui[k] = fmaf(kr, Cc.x, fmaf(ki, A.w, pui[k]));
+        if (H) {
+          phr[k] = fmaf(kr, B.w, fmaf(-ki, Cc.y, phr[k]));
+          phi[k] = fmaf(kr, Cc.y, fmaf(ki, B.w, phi[k]));
+        }
+      } else {
+        pur[k] = fmaf(kr, A.w, pur[k]);
+        if (H) phr[k] = fmaf(kr, B.w, phr[k]);
+      }
+    }
+  }
+}
+
+// s + c += p, with the rounding error of the sum carried in c (TwoSum).
+__device__ __forceinline__ void two_sum_add(float& s, float& c, float p) {
+  const float t = s + p;
+  const float z = t - s;
+  c += (s - (t - z)) + (p - z);
+  s = t;
+}
+
+struct TransArgs32 {
+  const int32_t* work_box;
+  const int32_t* work_row;
+  const int64_t* box_off;
+  const int32_t* box_rank;
+  const int64_t* list_off;
+  const int32_t* list_src;
+  const int8_t* list_kind;
+  const float4* hi32;
+  const float4* lo32;
+  const float4* geom32;
+  const float* q32;
+  const float* qhn32;
+  const float* qd32;
+  double* u;
+  double* uh;
+  float kappa;
+};
+
+template <int OP>
+__global__ void __launch_bounds__(kT32Threads) k_translate_f32(TransArgs32 a) {
+  constexpr bool C = OpTraits<OP>::kComplex;
+  constexpr int G = OpTraits<OP>::kGeom;
+  constexpr int TS = kTileSrcF32;
+  constexpr int RPT = kRowsPerThreadF32;
+  constexpr int W = C ? 2 : 1;
+  __shared__ float4 sA[TS];  // hx, hy, hz, c1r
+  __shared__ float4 sB[TS];  // lx, ly, lz, c2r
+  __shared__ float4 sC[(C || G == 1) ? TS : 1];  // c1i, c2i, gx, gy
+  __shared__ float sD[(G == 1) ? TS : 1];        // gz
+
+  const int U = a.work_box[blockIdx.x];
+  const int row0 = a.work_row[blockIdx.x];
+  const int64_t offU = a.box_off[U];
+  const int bsU = (int)(a.box_off[U + 1] - offU);
+  const int rU = a.box_rank[U];
+  const int rowt = row0 + RPT * threadIdx.x;  // first row of this thread
+
+  float4 th[RPT], tl[RPT], tg[RPT];
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int row = rowt + k;
+    const int64_t e = offU + (row < bsU ? row : bsU - 1);
+    th[k] = a.hi32[e];
+    tl[k] = a.lo32[e];
+    tg[k] = (G == 2) ? a.geom32[e] : make_float4(0, 0, 0, 0);
+  }
+  // skeleton rows need uh; decided per warp so the branch stays uniform
+  const bool need_h = (row0 + RPT * (threadIdx.x & ~31)) < rU;
+
+  // compensated FP32 accumulators: value s, error c
+  float sur[RPT], cur[RPT], sui[RPT], cui[RPT], shr[RPT], chr[RPT], shi[RPT], chi[RPT];
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) sur[k] = cur[k] = sui[k] = cui[k] = shr[k] = chr[k] = shi[k] = chi[k] = 0.f;
+
+  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
+  for (int64_t l = l0; l < l1; ++l) {
+    const int s = a.list_src[l];
+    const int kind = a.list_kind[l];
+    const int64_t offS = a.box_off[s];
+    const int bsS = (int)(a.box_off[s + 1] - offS);
+    const int rS = a.box_rank[s];
+    // sources [0, nh) carry a non-zero uh charge; tiles are cut at nh
+    const int nh = (kind == SKF_KIND_COLLEAGUE) ? rS : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
+    const bool self = (s == U);
+    const float* c1src = (kind == SKF_KIND_COARSE_DOWN) ? a.qd32 : a.q32;
+    for (int t0 = 0; t0 < bsS;) {
+      const bool hseg = t0 < nh;
+      const int nt = min(TS, (hseg ? nh : bsS) - t0);
+      __syncthreads();
+      for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        const int64_t e = offS + t0 + j;
+        const float4 h = a.hi32[e], lo = a.lo32[e];
+        float c1r = c1src[e * W], c1i = C ? c1src[e * W + 1] : 0.f;
+        float c2r = 0.f, c2i = 0.f;
+        if (kind == SKF_KIND_COLLEAGUE) {
+          c2r = a.qhn32[e * W];
+          if (C) c2i = a.qhn32[e * W + 1];
+        } else if (kind == SKF_KIND_COARSE_UP) {
+          c2r = -c1r;
+          c2i = -c1i;
+        }
+        sA[j] = make_float4(h.x, h.y, h.z, c1r);
+        sB[j] = make_float4(lo.x, lo.y, lo.z, c2r);
+        if (C || G == 1) {
+          const float4 g = (G == 1) ? a.geom32[e] : make_float4(0, 0, 0, 0);
+          sC[j] = make_float4(c1i, c2i, g.x, g.y);
+          if (G == 1) sD[j] = g.z;
+        }
+      }
+      __syncthreads();
+      float pur[RPT], pui[RPT], phr[RPT], phi[RPT];
+#pragma unroll
+      for (int k = 0; k < RPT; ++k) pur[k] = pui[k] = phr[k] = phi[k] = 0.f;
+      const bool doh = need_h && hseg;
+      if (doh) {
+        if (self) t32_tile<OP, true, true, RPT>(sA, sB, sC, sD, nt, th, tl, tg, a.kappa, pur, pui, phr, phi);
+        else t32_tile<OP, true, false, RPT>(sA, sB, sC, sD, nt, th, tl, tg, a.kappa, pur, pui, phr, phi);
+      } else {
+        if (self) t32_tile<OP, false, true, RPT>(sA, sB, sC, sD, nt, th, tl, tg, a.kappa, pur, pui, phr, phi);
+        else t32_tile<OP, false, false, RPT>(sA, sB, sC, sD, nt, th, tl, tg, a.kappa, pur, pui, phr, phi);
+      }
+#pragma unroll
+      for (int k = 0; k < RPT; ++k) {
+        two_sum_add(sur[k], cur[k], pur[k]);
+        if (C) two_sum_add(sui[k], cui[k], pui[k]);
+        if (doh) {
+          two_sum_add(shr[k], chr[k], phr[k]);
+          if (C) two_sum_add(shi[k], chi[k], phi[k]);
+        }
+      }
+      t0 += nt;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int row = rowt + k;
+    if (row >= bsU) continue;
+    const bool sk = row < rU;
+    const int64_t e = offU + row;
+    if (C) {
+      a.u[2 * e] = (double)sur[k] + (double)cur[k];
+      a.u[2 * e + 1] = (double)sui[k] + (double)cui[k];
+      a.uh[2 * e] = sk ? (double)shr[k] + (double)chr[k] : 0.0;
+      a.uh[2 * e + 1] = sk ? (double)shi[k] + (double)chi[k] : 0.0;
+    } else {
+      a.u[e] = (double)sur[k] + (double)cur[k];
+      a.uh[e] = sk ? (double)shr[k] + (double)chr[k] : 0.0;
+    }
+  }
+}
+
+}  // namespace skf
+
+namespace skf {
+
+// ------------------------------------------------------------------ mixed, packed FP32x2
+// Laplace 2D/3D translations with Blackwell's packed FP32x2 arithmetic
+// (add/mul/fma.rn.f32x2): every instruction works on two target rows, which
+// halves the issue slots per kernel evaluation; rsqrt/lg2 stay scalar (MUFU).
+// One warp per block, kX2Rows rows per thread (row0 + lane + 32 k), sources
+// staged in shared memory pre-negated and duplicated into both halves.
+// Same arithmetic per evaluation as k_translate_f32 (hi/lo differences,
+// compensated FP32 sums), so results agree with it to FP32 rounding order.
+typedef unsigned long long f2_t;  // two FP32 values in one 64-bit register
+
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
+  f2_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+  f2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+  f2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_pack(float lo, float hi) {
+  f2_t d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+__device__ __forceinline__ void f2_unpack(f2_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+constexpr int kX2Rows = 8;  // rows per thread (4 packed pairs)
+
+template <int D, bool H, bool SELF, bool LOG>
+__device__ __forceinline__ void x2_tile(const ulonglong2* __restrict__ s0, const ulonglong2* __restrict__ s1,
+                                        const ulonglong2* __restrict__ s2, const ulonglong2* __restrict__ s3, int nt,
+                                        const f2_t (&thx)[4], const f2_t (&thy)[4], const f2_t (&thz)[4],
+                                        const f2_t (&tlx)[4], const f2_t (&tly)[4], const f2_t (&tlz)[4],
+                                        f2_t (&pu)[4], f2_t (&ph)[4]) {
+#pragma unroll 2
+  for (int j = 0; j < nt; ++j) {
+    const ulonglong2 A = s0[j];  // (-hx,-hx), (-hy,-hy)
+    const ulonglong2 B = s1[j];  // (-hz,-hz), (-lx,-lx)
+    const ulonglong2 Cc = s2[j];  // (-ly,-ly), (-lz,-lz)
+    const ulonglong2 Q = s3[j];  // (c1,c1), (c2,c2)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const f2_t dx = f2_add(f2_add(thx[p], A.x), f2_add(tlx[p], B.y));
+      const f2_t dy = f2_add(f2_add(thy[p], A.y), f2_add(tly[p], Cc.x));
+      f2_t r2 = f2_mul(dx, dx);
+      r2 = f2_fma(dy, dy, r2);
+      if (D == 3) {
+        const f2_t dz = f2_add(f2_add(thz[p], B.x), f2_add(tlz[p], Cc.y));
+        r2 = f2_fma(dz, dz, r2);
+      }
+      float ra, rb;
+      f2_unpack(r2, ra, rb);
+      float ka = LOG ? lg2_approx(ra) : rsqrt_approx(ra);
+      float kb = LOG ? lg2_approx(rb) : rsqrt_approx(rb);
+      if (SELF) {
+        ka = ra > 0.f ? ka : 0.f;
+        kb = rb > 0.f ? kb : 0.f;
+      }
+      const f2_t k = f2_pack(ka, kb);
+      pu[p] = f2_fma(k, Q.x, pu[p]);
+      if (H) ph[p] = f2_fma(k, Q.y, ph[p]);
+    }
+  }
+}
+
+// s + c += p for both halves (TwoSum, see two_sum_add).
+__device__ __forceinline__ void f2_two_sum(f2_t& s, f2_t& c, f2_t p) {
+  const f2_t t = f2_add(s, p);
+  const f2_t neg = f2_pack(-1.f, -1.f);
+  const f2_t z = f2_fma(s, neg, t);                     // t - s
+  const f2_t tz = f2_fma(z, neg, t);                    // t - z
+  const f2_t e = f2_add(f2_fma(tz, neg, s), f2_fma(z, neg, p));  // (s - (t - z)) + (p - z)
+  c = f2_add(c, e);
+  s = t;
+}
+
+template <int OP>
+__global__ void __launch_bounds__(32) k_translate_f32x2(TransArgs32 a) {
+  constexpr int D = OpTraits<OP>::kDim;
+  constexpr bool LOG = (OP == SKF_LAPLACE_2D);
+  constexpr int TS = kTileSrcF32;
+  __shared__ ulonglong2 s0[TS], s1[TS], s2[TS], s3[TS];
+
+  const int lane = threadIdx.x;
+  const int U = a.work_box[blockIdx.x];
+  const int row0 = a.work_row[blockIdx.x];
+  const int64_t offU = a.box_off[U];
+  const int bsU = (int)(a.box_off[U + 1] - offU);
+  const int rU = a.box_rank[U];
+
+  f2_t thx[4], thy[4], thz[4], tlx[4], tly[4], tlz[4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int ra = row0 + lane + 32 * (2 * p), rb = ra + 32;
+    const float4 ha = a.hi32[offU + min(ra, bsU - 1)], hb = a.hi32[offU + min(rb, bsU - 1)];
+    const float4 la = a.lo32[offU + min(ra, bsU - 1)], lb = a.lo32[offU + min(rb, bsU - 1)];
+    thx[p] = f2_pack(ha.x, hb.x);
+    thy[p] = f2_pack(ha.y, hb.y);
+    thz[p] = f2_pack(ha.z, hb.z);
+    tlx[p] = f2_pack(la.x, lb.x);
+    tly[p] = f2_pack(la.y, lb.y);
+    tlz[p] = f2_pack(la.z, lb.z);
+  }
+  const bool need_h = row0 < rU;
+  const f2_t zero = f2_pack(0.f, 0.f);
+  f2_t su[4], cu[4], sh[4], ch[4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p) su[p] = cu[p] = sh[p] = ch[p] = zero;
+
+  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
+  for (int64_t l = l0; l < l1; ++l) {
+    const int s = a.list_src[l];
+    const int kind = a.list_kind[l];
+    const int64_t offS = a.box_off[s];
+    const int bsS = (int)(a.box_off[s + 1] - offS);
+    const int rS = a.box_rank[s];
+    const int nh = (kind == SKF_KIND_COLLEAGUE) ? rS : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
+    const bool self = (s == U);
+    const float* c1src = (kind == SKF_KIND_COARSE_DOWN) ? a.qd32 : a.q32;
+    for (int t0 = 0; t0 < bsS;) {
+      const bool hseg = t0 < nh;
+      const int nt = min(TS, (hseg ? nh : bsS) - t0);
+      __syncwarp();
+      for (int j = lane; j < nt; j += 32) {
+        const int64_t e = offS + t0 + j;
+        const float4 h = a.hi32[e], lo = a.lo32[e];
+        const float c1 = c1src[e];
+        float c2 = 0.f;
+        if (kind == SKF_KIND_COLLEAGUE) c2 = a.qhn32[e];
+        else if (kind == SKF_KIND_COARSE_UP) c2 = -c1;
+        s0[j] = make_ulonglong2(f2_pack(-h.x, -h.x), f2_pack(-h.y, -h.y));
+        s1[j] = make_ulonglong2(f2_pack(-h.z, -h.z), f2_pack(-lo.x, -lo.x));
+        s2[j] = make_ulonglong2(f2_pack(-lo.y, -lo.y), f2_pack(-lo.z, -lo.z));
+        s3[j] = make_ulonglong2(f2_pack(c1, c1), f2_pack(c2, c2));
+      }
+      __syncwarp();
+      f2_t pu[4], ph[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) pu[p] = ph[p] = zero;
+      const bool doh = need_h && hseg;
+      if (doh) {
+        if (self) x2_tile<D, true, true, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
+        else x2_tile<D, true, false, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
+      } else {
+        if (self) x2_tile<D, false, true, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
+        else x2_tile<D, false, false, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        f2_two_sum(su[p], cu[p], pu[p]);
+        if (doh) f2_two_sum(sh[p], ch[p], ph[p]);
+      }
+      t0 += nt;
+    }
+  }
+  // log r = (ln 2 / 2) log2(r^2): the constant is applied once to the sums
+  const double scale = LOG ? 0.34657359027997264 : 1.0;
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    float sua, sub, cua, cub, sha, shb, cha, chb;
+    f2_unpack(su[p], sua, sub);
+    f2_unpack(cu[p], cua, cub);
+    f2_unpack(sh[p], sha, shb);
+    f2_unpack(ch[p], cha, chb);
+    const int ra = row0 + lane + 32 * (2 * p), rb = ra + 32;
+    if (ra < bsU) {
+      a.u[offU + ra] = scale * ((double)sua + (double)cua);
+      a.uh[offU + ra] = ra < rU ? scale * ((double)sha + (double)cha) : 0.0;
+    }
+    if (rb < bsU) {
+      a.u[offU + rb] = scale * ((double)sub + (double)cub);
+      a.uh[offU + rb] = rb < rU ? scale * ((double)shb + (double)chb) : 0.0;
+    }
+  }
+}
+
+}  // namespace skf

@@ -221,6 +221,9 @@ class Plan:
                                                    None if stream is None else ctypes.c_void_p(stream)),
                    "skf_plan_apply_host")
 
+    def set_option(self, option, value):
+        _lib.check(_lib.load().skf_plan_set_option(self._h, int(option), int(value)), "skf_plan_set_option")
+
     def time_translations(self, precision, reps=5, stream=None):
         ms = ctypes.c_float()
         _lib.check(_lib.load().skf_plan_time_translations(self._h, int(precision), int(reps),
