@@ -115,6 +115,9 @@ int skf_plan_apply_host(skf_plan* plan, const void* x_host, void* y_host, int32_
    scalar FP32 kernel even where the packed FP32x2 kernel exists (Laplace), 0 =
    default.  Used to cross-check the two kernels. */
 #define SKF_OPT_SCALAR_MIXED 1
+/* SKF_OPT_PACKED_SHAPE: block shape of the packed kernel, 0 = 4 warps x 1 row
+   pair per thread (default), 1 = 1 warp x 4 pairs, 2 = 2 warps x 2 pairs. */
+#define SKF_OPT_PACKED_SHAPE 2
 int skf_plan_set_option(skf_plan* plan, int32_t option, int64_t value);
 
 /* Time the plan's translation kernel alone (device time in ms over `reps`

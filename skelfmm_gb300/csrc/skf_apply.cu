@@ -239,11 +239,16 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
     b.u = p->u;
     b.uh = p->uh;
     b.kappa = (float)p->kappa;
-    static_assert(32 * kX2Rows == kT32Threads * kRowsPerThreadF32, "work tiles are shared by both mixed kernels");
+    static_assert(kT32Threads * kRowsPerThreadF32 == 256, "mixed work items are 256-row tiles");
     if (p->work32.n > 0) {
       if constexpr (OP == SKF_LAPLACE_2D || OP == SKF_LAPLACE_3D) {
         if (!p->scalar_mixed) {
-          k_translate_f32x2<OP><<<p->work32.n, 32, 0, st>>>(b);
+          // packed kernel geometry: warps per block x row pairs per thread
+          switch (p->x2_config) {
+            case 1: k_translate_f32x2<OP, 1, 4><<<p->work32.n, 32, 0, st>>>(b); break;
+            case 2: k_translate_f32x2<OP, 2, 2><<<p->work32.n, 64, 0, st>>>(b); break;
+            default: k_translate_f32x2<OP, 4, 1><<<p->work32.n, 128, 0, st>>>(b); break;
+          }
           return;
         }
       }

@@ -50,6 +50,7 @@ struct skf_plan {
   int op = 0, ndim = 3, nboxes = 0, nlevels = 0, root_level = 0;
   bool cplx = false;
   bool scalar_mixed = false;  // force the scalar FP32 translation kernel (comparison/testing)
+  int x2_config = 0;          // packed kernel: 0 = 4 warps x 1 pair, 1 = 1 x 4, 2 = 2 x 2
   double kappa = 0.0;
   int64_t E = 0, N = 0, nperm = 0, t_len = 0, nlist = 0;
   int64_t pairs = 0;  // kernel evaluations per apply

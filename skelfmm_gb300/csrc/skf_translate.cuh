@@ -405,22 +405,22 @@ __device__ __forceinline__ void f2_unpack(f2_t v, float& lo, float& hi) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
 }
 
-constexpr int kX2Rows = 8;  // rows per thread (4 packed pairs)
-
-template <int D, bool H, bool SELF, bool LOG>
+// NP packed row pairs per thread: lane l of warp w owns rows
+// row0 + 64 NP w + 32 k + l, k < 2 NP; row pair p = (k = 2p, 2p + 1).
+template <int D, int NP, bool H, bool SELF, bool LOG>
 __device__ __forceinline__ void x2_tile(const ulonglong2* __restrict__ s0, const ulonglong2* __restrict__ s1,
                                         const ulonglong2* __restrict__ s2, const ulonglong2* __restrict__ s3, int nt,
-                                        const f2_t (&thx)[4], const f2_t (&thy)[4], const f2_t (&thz)[4],
-                                        const f2_t (&tlx)[4], const f2_t (&tly)[4], const f2_t (&tlz)[4],
-                                        f2_t (&pu)[4], f2_t (&ph)[4]) {
-#pragma unroll 2
+                                        const f2_t (&thx)[NP], const f2_t (&thy)[NP], const f2_t (&thz)[NP],
+                                        const f2_t (&tlx)[NP], const f2_t (&tly)[NP], const f2_t (&tlz)[NP],
+                                        f2_t (&pu)[NP], f2_t (&ph)[NP]) {
+#pragma unroll 4
   for (int j = 0; j < nt; ++j) {
-    const ulonglong2 A = s0[j];  // (-hx,-hx), (-hy,-hy)
-    const ulonglong2 B = s1[j];  // (-hz,-hz), (-lx,-lx)
+    const ulonglong2 A = s0[j];   // (-hx,-hx), (-hy,-hy)
+    const ulonglong2 B = s1[j];   // (-hz,-hz), (-lx,-lx)
     const ulonglong2 Cc = s2[j];  // (-ly,-ly), (-lz,-lz)
-    const ulonglong2 Q = s3[j];  // (c1,c1), (c2,c2)
+    const ulonglong2 Q = s3[j];   // (c1,c1), (c2,c2)
 #pragma unroll
-    for (int p = 0; p < 4; ++p) {
+    for (int p = 0; p < NP; ++p) {
       const f2_t dx = f2_add(f2_add(thx[p], A.x), f2_add(tlx[p], B.y));
       const f2_t dy = f2_add(f2_add(thy[p], A.y), f2_add(tly[p], Cc.x));
       f2_t r2 = f2_mul(dx, dx);
@@ -448,33 +448,40 @@ __device__ __forceinline__ void x2_tile(const ulonglong2* __restrict__ s0, const
 __device__ __forceinline__ void f2_two_sum(f2_t& s, f2_t& c, f2_t p) {
   const f2_t t = f2_add(s, p);
   const f2_t neg = f2_pack(-1.f, -1.f);
-  const f2_t z = f2_fma(s, neg, t);                     // t - s
-  const f2_t tz = f2_fma(z, neg, t);                    // t - z
+  const f2_t z = f2_fma(s, neg, t);                               // t - s
+  const f2_t tz = f2_fma(z, neg, t);                              // t - z
   const f2_t e = f2_add(f2_fma(tz, neg, s), f2_fma(z, neg, p));  // (s - (t - z)) + (p - z)
   c = f2_add(c, e);
   s = t;
 }
 
-template <int OP>
-__global__ void __launch_bounds__(32) k_translate_f32x2(TransArgs32 a) {
+// NW warps per block share one staged source tile; a block covers
+// 64 NW NP = 256 rows.  Warps whose rows all lie past the box skip the
+// arithmetic, so a partial tile wastes at most 63 rows.
+template <int OP, int NW, int NP>
+__global__ void __launch_bounds__(NW * 32) k_translate_f32x2(TransArgs32 a) {
   constexpr int D = OpTraits<OP>::kDim;
   constexpr bool LOG = (OP == SKF_LAPLACE_2D);
   constexpr int TS = kTileSrcF32;
+  static_assert(64 * NW * NP == 256, "work items are 256-row tiles");
   __shared__ ulonglong2 s0[TS], s1[TS], s2[TS], s3[TS];
 
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int U = a.work_box[blockIdx.x];
   const int row0 = a.work_row[blockIdx.x];
   const int64_t offU = a.box_off[U];
   const int bsU = (int)(a.box_off[U + 1] - offU);
   const int rU = a.box_rank[U];
+  const int wrow0 = row0 + 64 * NP * warp;  // first row of this warp
+  const bool active = wrow0 < bsU;
 
-  f2_t thx[4], thy[4], thz[4], tlx[4], tly[4], tlz[4];
+  f2_t thx[NP], thy[NP], thz[NP], tlx[NP], tly[NP], tlz[NP];
 #pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    const int ra = row0 + lane + 32 * (2 * p), rb = ra + 32;
-    const float4 ha = a.hi32[offU + min(ra, bsU - 1)], hb = a.hi32[offU + min(rb, bsU - 1)];
-    const float4 la = a.lo32[offU + min(ra, bsU - 1)], lb = a.lo32[offU + min(rb, bsU - 1)];
+  for (int p = 0; p < NP; ++p) {
+    const int ra = wrow0 + lane + 64 * p, rb = ra + 32;
+    const int64_t ea = offU + max(0, min(ra, bsU - 1)), eb = offU + max(0, min(rb, bsU - 1));
+    const float4 ha = a.hi32[ea], hb = a.hi32[eb];
+    const float4 la = a.lo32[ea], lb = a.lo32[eb];
     thx[p] = f2_pack(ha.x, hb.x);
     thy[p] = f2_pack(ha.y, hb.y);
     thz[p] = f2_pack(ha.z, hb.z);
@@ -482,11 +489,11 @@ __global__ void __launch_bounds__(32) k_translate_f32x2(TransArgs32 a) {
     tly[p] = f2_pack(la.y, lb.y);
     tlz[p] = f2_pack(la.z, lb.z);
   }
-  const bool need_h = row0 < rU;
+  const bool need_h = wrow0 < rU;
   const f2_t zero = f2_pack(0.f, 0.f);
-  f2_t su[4], cu[4], sh[4], ch[4];
+  f2_t su[NP], cu[NP], sh[NP], ch[NP];
 #pragma unroll
-  for (int p = 0; p < 4; ++p) su[p] = cu[p] = sh[p] = ch[p] = zero;
+  for (int p = 0; p < NP; ++p) su[p] = cu[p] = sh[p] = ch[p] = zero;
 
   const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
   for (int64_t l = l0; l < l1; ++l) {
@@ -501,8 +508,8 @@ __global__ void __launch_bounds__(32) k_translate_f32x2(TransArgs32 a) {
     for (int t0 = 0; t0 < bsS;) {
       const bool hseg = t0 < nh;
       const int nt = min(TS, (hseg ? nh : bsS) - t0);
-      __syncwarp();
-      for (int j = lane; j < nt; j += 32) {
+      __syncthreads();
+      for (int j = threadIdx.x; j < nt; j += NW * 32) {
         const int64_t e = offS + t0 + j;
         const float4 h = a.hi32[e], lo = a.lo32[e];
         const float c1 = c1src[e];
@@ -514,36 +521,39 @@ __global__ void __launch_bounds__(32) k_translate_f32x2(TransArgs32 a) {
         s2[j] = make_ulonglong2(f2_pack(-lo.y, -lo.y), f2_pack(-lo.z, -lo.z));
         s3[j] = make_ulonglong2(f2_pack(c1, c1), f2_pack(c2, c2));
       }
-      __syncwarp();
-      f2_t pu[4], ph[4];
+      __syncthreads();
+      if (active) {
+        f2_t pu[NP], ph[NP];
 #pragma unroll
-      for (int p = 0; p < 4; ++p) pu[p] = ph[p] = zero;
-      const bool doh = need_h && hseg;
-      if (doh) {
-        if (self) x2_tile<D, true, true, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
-        else x2_tile<D, true, false, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
-      } else {
-        if (self) x2_tile<D, false, true, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
-        else x2_tile<D, false, false, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
-      }
+        for (int p = 0; p < NP; ++p) pu[p] = ph[p] = zero;
+        const bool doh = need_h && hseg;
+        if (doh) {
+          if (self) x2_tile<D, NP, true, true, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
+          else x2_tile<D, NP, true, false, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
+        } else {
+          if (self) x2_tile<D, NP, false, true, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
+          else x2_tile<D, NP, false, false, LOG>(s0, s1, s2, s3, nt, thx, thy, thz, tlx, tly, tlz, pu, ph);
+        }
 #pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        f2_two_sum(su[p], cu[p], pu[p]);
-        if (doh) f2_two_sum(sh[p], ch[p], ph[p]);
+        for (int p = 0; p < NP; ++p) {
+          f2_two_sum(su[p], cu[p], pu[p]);
+          if (doh) f2_two_sum(sh[p], ch[p], ph[p]);
+        }
       }
       t0 += nt;
     }
   }
+  if (!active) return;
   // log r = (ln 2 / 2) log2(r^2): the constant is applied once to the sums
   const double scale = LOG ? 0.34657359027997264 : 1.0;
 #pragma unroll
-  for (int p = 0; p < 4; ++p) {
+  for (int p = 0; p < NP; ++p) {
     float sua, sub, cua, cub, sha, shb, cha, chb;
     f2_unpack(su[p], sua, sub);
     f2_unpack(cu[p], cua, cub);
     f2_unpack(sh[p], sha, shb);
     f2_unpack(ch[p], cha, chb);
-    const int ra = row0 + lane + 32 * (2 * p), rb = ra + 32;
+    const int ra = wrow0 + lane + 64 * p, rb = ra + 32;
     if (ra < bsU) {
       a.u[offU + ra] = scale * ((double)sua + (double)cua);
       a.uh[offU + ra] = ra < rU ? scale * ((double)sha + (double)cha) : 0.0;

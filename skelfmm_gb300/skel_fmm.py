@@ -187,22 +187,35 @@ class SkelFMM:
         idx = np.asarray(indices, dtype=np.int64)
         cplx = is_complex_op(self.operator)
         dev = self.device
-        src = torch.from_numpy(self.points).to(dev).unsqueeze(0)
-        xq = torch.from_numpy(np.ascontiguousarray(x, dtype=np.complex128 if cplx else np.float64)).to(dev)
-        gs = gt = None
+        n = self.points.shape[0]
+        # sources split into chunks, one batched "pair" per chunk, so the sum
+        # spreads over the whole GPU; partial sums are added in FP64
+        nchunk = max(1, min(1024, n // 4096))
+        csz = -(-n // nchunk)
+        pad = nchunk * csz - n
+        pts = np.concatenate((self.points, np.zeros((pad, self.points.shape[1]))))
+        xv = np.concatenate((np.asarray(x, dtype=np.complex128 if cplx else np.float64),
+                             np.zeros(pad, dtype=np.complex128 if cplx else np.float64)))
+        src = torch.from_numpy(pts.reshape(nchunk, csz, -1)).to(dev)
+        xq = torch.from_numpy(xv.reshape(nchunk, csz, 1)).to(dev)
+        ncnt = torch.full((nchunk,), csz, dtype=torch.int32, device=dev)
+        ncnt[-1] = csz - pad
+        gs = None
         if self.operator.geometry_side == "source":
-            gs = torch.from_numpy(np.ascontiguousarray(self.geometry, dtype=np.float64)).to(dev).unsqueeze(0)
+            g = np.concatenate((self.geometry, np.zeros((pad, 3))))
+            gs = torch.from_numpy(np.ascontiguousarray(g, dtype=np.float64).reshape(nchunk, csz, 3)).to(dev)
         out = []
-        for s in range(0, idx.shape[0], 4096):
-            t = idx[s: s + 4096]
-            trg = torch.from_numpy(np.ascontiguousarray(self.points[t])).to(dev).unsqueeze(0)
+        for s in range(0, idx.shape[0], 2048):
+            t = idx[s: s + 2048]
+            trg = torch.from_numpy(np.ascontiguousarray(self.points[t])).to(dev).unsqueeze(0).expand(nchunk, -1, -1)
             gtt = None
             if self.operator.geometry_side == "target":
-                gtt = torch.from_numpy(np.ascontiguousarray(self.geometry[t], dtype=np.float64)).to(dev).unsqueeze(0)
+                gtt = torch.from_numpy(np.ascontiguousarray(self.geometry[t], dtype=np.float64)).to(dev)
+                gtt = gtt.unsqueeze(0).expand(nchunk, -1, -1)
             # a coincident pair contributes 0, as in the dense kernels
-            out.append(batched_kernel_apply(cuda_op_id(self.operator), xq.unsqueeze(0).unsqueeze(-1), trg, src,
-                                            param=self.param, geom_trg=gtt if gtt is not None else gt,
-                                            geom_src=gs)[0, :, 0].cpu().numpy())
+            part = batched_kernel_apply(cuda_op_id(self.operator), xq, trg, src, param=self.param, geom_trg=gtt,
+                                        geom_src=gs, n=ncnt)
+            out.append(part.sum(dim=0)[:, 0].cpu().numpy())
         return np.concatenate(out)
 
     def relerr_fmm_apply_check(self, x, *, ncheck=64, seed=0, indices=None):
