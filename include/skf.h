@@ -151,6 +151,26 @@ int skf_skel_boxes(int32_t op, double kappa, int32_t nbox, const int64_t* off, c
                    double tol, int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out,
                    void* stream);
 
+/*
+ * skf_skel_boxes without any device allocation.  No counterpart in the
+ * reference: for callers that may not allocate GPU memory on this code path
+ * (their own pool owns the device memory, a host framework's fixed budget, a
+ * latency-bound loop).  Same arguments and outputs as skf_skel_boxes; the
+ * workspace is a fixed file-scope device array of SKF_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading the library keeps until exit.  A box whose FP64
+ * proxy matrix (rows x box size, x2 when complex) does not fit returns
+ * SKF_ERR_SCRATCH before any work.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) and should precede any stream
+ * capture on that device.  All calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller.
+ */
+#define SKF_NOALLOC_SCRATCH_BYTES (64ll << 20)
+#define SKF_ERR_SCRATCH 7 /* problem exceeds the fixed no-allocation scratch */
+int skf_skel_boxes_noalloc(int32_t op, double kappa, int32_t nbox, const int64_t* off, const double* x,
+                           const double* geom, const double* centers, double box_length, int32_t nproxy,
+                           double tol, int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out,
+                           void* stream);
+
 const char* skf_status_string(int32_t status);
 int skf_version(void);
 

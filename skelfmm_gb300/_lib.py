@@ -20,6 +20,7 @@ SKF_ERR_CUDA = 3
 SKF_ERR_UNSUPPORTED = 4
 SKF_ERR_ID = 5
 SKF_ERR_TIMEOUT = 6
+SKF_ERR_SCRATCH = 7
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -68,6 +69,7 @@ SIGNATURES = {
     "skf_plan_time_translations": (_i32, [_p, _i32, _i32, _p, ctypes.POINTER(ctypes.c_float)]),
     "skf_kernel_apply": (_i32, [_i32, _f64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p, _p, _p, _p, _i32, _p]),
     "skf_skel_boxes": (_i32, [_i32, _f64, _i32, _p, _p, _p, _p, _f64, _i32, _f64, _p, _p, _p, _p, _p]),
+    "skf_skel_boxes_noalloc": (_i32, [_i32, _f64, _i32, _p, _p, _p, _p, _f64, _i32, _f64, _p, _p, _p, _p, _p]),
 }
 
 _lib = None

@@ -534,4 +534,91 @@ int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double*
   return status;
 }
 
+// Same work as skel_boxes, with the proxy template, the per-box workspace
+// offsets and the workspaces carved out of a caller-provided device buffer of
+// `cap` doubles instead of stream-ordered allocations.  Boxes are processed
+// in batches that fit the buffer, in stream order.  Returns SKF_ERR_SCRATCH,
+// before any device work, when one box's proxy matrix does not fit.
+int skel_boxes_scratch(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
+                       const double* centers, double box_length, int nproxy, double tol, int32_t* rank,
+                       int32_t* perm, const int64_t* t_off_out, void* t_out, double* scratch, int64_t cap,
+                       cudaStream_t st) {
+  const int ndim = (op == SKF_LAPLACE_2D || op == SKF_HELMHOLTZ_2D) ? 2 : 3;
+  const bool geom_op = op >= SKF_LAPLACE_DOUBLE_LAYER_3D;
+  const bool cplx = op == SKF_HELMHOLTZ_2D || op == SKF_HELMHOLTZ_3D || op == SKF_HELMHOLTZ_DOUBLE_LAYER_3D ||
+                    op == SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D;
+  const int W = cplx ? 2 : 1;
+  std::vector<double> tmpl = proxy_template(ndim, geom_op, nproxy);
+  const int np = (int)(tmpl.size() / ndim);
+  const int mrows = geom_op ? 2 * np : np;
+  constexpr int64_t kMaxBatch = 4096;  // workspace-offset slots
+  const int64_t tsz = ((int64_t)tmpl.size() + 31) / 32 * 32;
+  const int64_t wcap = cap - tsz - kMaxBatch;
+  if (wcap <= 0) return SKF_ERR_SCRATCH;
+  std::vector<int64_t> hoff(nbox + 1);
+  SKF_CUDA_TRY(cudaMemcpyAsync(hoff.data(), off, sizeof(int64_t) * (nbox + 1), cudaMemcpyDeviceToHost, st));
+  SKF_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int b = 0; b < nbox; ++b)
+    if ((int64_t)mrows * (hoff[b + 1] - hoff[b]) * W > wcap) return SKF_ERR_SCRATCH;
+
+  double* dtmpl = scratch;
+  int64_t* dwso = reinterpret_cast<int64_t*>(scratch + tsz);
+  double* ws = scratch + tsz + kMaxBatch;
+  SKF_CUDA_TRY(cudaMemcpyAsync(dtmpl, tmpl.data(), sizeof(double) * tmpl.size(), cudaMemcpyHostToDevice, st));
+  int status = SKF_OK;
+  int b0 = 0;
+  while (b0 < nbox && status == SKF_OK) {
+    std::vector<int64_t> wso;
+    int64_t acc = 0;
+    int b1 = b0;
+    while (b1 < nbox && (int64_t)wso.size() < kMaxBatch) {
+      const int64_t need = (int64_t)mrows * (hoff[b1 + 1] - hoff[b1]) * W;
+      if (acc + need > wcap) break;
+      wso.push_back(acc);
+      acc += need;
+      ++b1;
+    }
+    // pageable source: the copy is staged before this call returns, and it is
+    // ordered after the previous batch's kernel on the stream
+    SKF_CUDA_TRY(cudaMemcpyAsync(dwso, wso.data(), sizeof(int64_t) * wso.size(), cudaMemcpyHostToDevice, st));
+    SkelArgs a;
+    a.off = off;
+    a.x = x;
+    a.geom = geom;
+    a.centers = centers;
+    a.tmpl = dtmpl;
+    a.np = np;
+    a.mrows = mrows;
+    a.plen = 2.95 * box_length;
+    a.kappa = kappa;
+    a.tol = tol;
+    a.ws = ws;
+    a.ws_off = dwso;
+    a.rank = rank;
+    a.perm = perm;
+    a.t_off_out = t_off_out;
+    a.t_out = static_cast<double*>(t_out);
+    a.first_box = b0;
+    int maxn_batch = 1;
+    for (int b = b0; b < b1; ++b) maxn_batch = std::max<int>(maxn_batch, (int)(hoff[b + 1] - hoff[b]));
+    switch (op) {
+#define SKF_CASE(OPID) \
+  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, st); break;
+      SKF_CASE(SKF_LAPLACE_2D)
+      SKF_CASE(SKF_LAPLACE_3D)
+      SKF_CASE(SKF_HELMHOLTZ_2D)
+      SKF_CASE(SKF_HELMHOLTZ_3D)
+      SKF_CASE(SKF_LAPLACE_DOUBLE_LAYER_3D)
+      SKF_CASE(SKF_LAPLACE_ADJOINT_DOUBLE_LAYER_3D)
+      SKF_CASE(SKF_HELMHOLTZ_DOUBLE_LAYER_3D)
+      SKF_CASE(SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D)
+#undef SKF_CASE
+      default: status = SKF_ERR_ARG;
+    }
+    b0 = b1;
+  }
+  if (status == SKF_OK) SKF_CUDA_TRY(cudaGetLastError());
+  return status;
+}
+
 }  // namespace skf
