@@ -185,6 +185,8 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
+    # first use of the library/CUDA context outside the timed build
+    SkelFMM(pts[:2000], operators.LAPLACE_3D, tol=args.tol, leaf_size=args.leaf, precision="mixed")
     barrier()
     t0 = time.perf_counter()
     f = SkelFMM(pts, operators.LAPLACE_3D, tol=args.tol, leaf_size=args.leaf, precision="mixed")
@@ -253,20 +255,25 @@ def run_ours(args):
     err_mixed = float(np.abs(ymix[idx] - yd).max() / den)
     err_fp64 = None if y64 is None else float(np.abs(y64[idx] - yd).max() / den)
 
-    # roofline of the dominant kernel (translations, mixed): kernel pair
-    # evaluations per launch over the launch's device time, against the MUFU
-    # issue rate (one rsqrt per pair): 152 SMs x 16 per clock x max SM clock
+    # roofline of the dominant kernel (translations, mixed): algorithmic kernel
+    # pair evaluations per launch (counted from the built lists) over the
+    # launch's device time.  Per pair the algorithm needs 7 FP32 FMA-pipe ops
+    # (3 sub, 3 FMA for r^2, 1 FMA accumulate) and 1 rsqrt on the XU pipe.
+    # GB300: 128 FMA-pipe lanes/clk/SM; the XU pipe issues 32 lanes/clk/SM
+    # (ncu pct_of_peak of sm__inst_executed_pipe_xu), so the FMA pipe binds:
+    # peak = 152 SMs x 128/7 pairs/clk x max SM clock.
     peaks, src = measured_peaks()
     t_ms = plan.time_translations(_lib.PREC_MIXED, reps=5, stream=sp)
     pairs = int(plan.info.npairs_fused)
     achieved = pairs / (t_ms * 1e-3) / 1e9
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    peak = 152 * 16 * sm_mhz * 1e6 / 1e9
+    peak = 152 * (128.0 / 7.0) * sm_mhz * 1e6 / 1e9
     roofline = {
-        "bound": "mufu", "kernel": "k_translate_f32<LAPLACE_3D>", "achieved": round(achieved, 1),
+        "bound": "fp32-fma", "kernel": "k_translate_f32x2<LAPLACE_3D>", "achieved": round(achieved, 1),
         "peak": round(peak, 1), "unit": "Gpair/s", "frac": round(achieved / peak, 4),
         "traffic": profiled_traffic("translate_lap3d_1M.md"),
-        "peak_source": f"152 SMs x 16 MUFU/clk x sm_max_mhz {sm_mhz:.0f} ({src} MEASURED_PEAKS.json clock)",
+        "peak_source": f"152 SMs x 128/7 pairs/clk (FP32 FMA pipe, 7 ops/pair) x sm_max_mhz {sm_mhz:.0f} "
+                       f"({src} MEASURED_PEAKS.json clock); XU (rsqrt) 32/clk/SM is not binding",
         "pairs_per_launch": pairs, "launch_ms": round(t_ms, 4),
     }
     cpu = None
