@@ -97,6 +97,8 @@ typedef struct {
   int64_t device_bytes;   /* bytes the plan holds on the device */
   int32_t nwork;          /* translation work items */
   int32_t is_complex;
+  int64_t npairs_evaluated_mixed; /* kernel evaluations the mixed apply performs
+                                     (fewer than npairs_fused on the symmetric path) */
 } skf_plan_info;
 
 int skf_plan_create(const skf_plan_desc* desc, skf_plan** out);
@@ -118,6 +120,9 @@ int skf_plan_apply_host(skf_plan* plan, const void* x_host, void* y_host, int32_
 /* SKF_OPT_PACKED_SHAPE: block shape of the packed kernel, 0 = 4 warps x 1 row
    pair per thread (default), 1 = 1 warp x 4 pairs, 2 = 2 warps x 2 pairs. */
 #define SKF_OPT_PACKED_SHAPE 2
+/* SKF_OPT_SYMMETRIC: 1 (default) = for symmetric point kernels with symmetric
+   lists, evaluate each kernel block once for both directions; 0 = off. */
+#define SKF_OPT_SYMMETRIC 3
 int skf_plan_set_option(skf_plan* plan, int32_t option, int64_t value);
 
 /* Time the plan's translation kernel alone (device time in ms over `reps`

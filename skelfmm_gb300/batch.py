@@ -1,0 +1,179 @@
+"""Many independent FMM instances applied as one operator.
+
+Instances (uneven sizes, adaptive trees, different skeleton ranks) are built
+separately and then concatenated into a single ragged plan: boxes, entries,
+interaction lists and interpolation blocks of all instances live in one CSR
+layout, so one apply runs every phase (permute, upward T per level, the
+translations of all levels, downward T^T, permute) for all instances with a
+single launch per phase.  Levels are aligned at each instance's root level.
+The apply can be captured once into a CUDA graph and replayed.
+
+An autotuner picks, per plan, the translation scheme (symmetric or
+per-direction) and the packed kernel's block shape by timing them.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .operators import is_complex_op
+from .plan import Plan, RaggedBuild
+from .recursive_skel import RecursiveSkeletonization
+from .skel_fmm import direct_sum
+from .tree import BalancedTree
+
+
+def concat_ragged(rbs):
+    """One ragged build holding every instance; instance i's points occupy
+    rows [starts[i], starts[i+1]) of the concatenated input vector."""
+    op = rbs[0].op
+    if any(rb.op != op or rb.ndim != rbs[0].ndim or rb.kappa != rbs[0].kappa for rb in rbs):
+        raise ValueError("instances must share the operator, dimension and kappa")
+    R = max(rb.root_level for rb in rbs)
+    nlev = max(rb.nlevels - rb.root_level for rb in rbs) + R
+    box_level, box_rank, box_off = [], [], [np.zeros(1, np.int64)]
+    xyz, geom, pslot, pe, pp, t_off, t_data = [], [], [], [], [], [], []
+    list_off, list_src, list_kind = [np.zeros(1, np.int64)], [], []
+    eoff = boff = poff = toff = loff = 0
+    starts = [0]
+    for rb in rbs:
+        nb = rb.nboxes
+        box_level.append(np.maximum(rb.box_level.astype(np.int64) - rb.root_level + R, 0).astype(np.int32))
+        box_rank.append(rb.box_rank)
+        box_off.append(rb.box_off[1:] + eoff)
+        xyz.append(rb.entry_xyz)
+        if rb.entry_geom is not None:
+            geom.append(rb.entry_geom)
+        pslot.append(np.where(rb.entry_pslot >= 0, rb.entry_pslot + eoff, -1))
+        pe.append(rb.perm_entry + eoff)
+        pp.append(rb.perm_point + poff)
+        t_off.append(np.where(rb.t_off >= 0, rb.t_off + toff, -1))
+        t_data.append(rb.t_data)
+        list_off.append(rb.list_off[1:] + loff)
+        list_src.append(rb.list_src.astype(np.int64) + boff)
+        list_kind.append(rb.list_kind)
+        eoff += rb.nentries
+        boff += nb
+        poff += rb.npoints
+        toff += rb.t_data.shape[0]
+        loff += int(rb.list_off[-1])
+        starts.append(poff)
+    out = RaggedBuild(
+        op=op, ndim=rbs[0].ndim, kappa=rbs[0].kappa, npoints=int(poff), nlevels=int(nlev), root_level=int(R),
+        box_level=np.concatenate(box_level), box_off=np.concatenate(box_off), box_rank=np.concatenate(box_rank),
+        entry_xyz=np.concatenate(xyz), entry_geom=np.concatenate(geom) if geom else None,
+        entry_pslot=np.concatenate(pslot), perm_entry=np.concatenate(pe), perm_point=np.concatenate(pp),
+        t_off=np.concatenate(t_off), t_data=np.concatenate(t_data), list_off=np.concatenate(list_off),
+        list_src=np.concatenate(list_src).astype(np.int32), list_kind=np.concatenate(list_kind),
+    )
+    return out, np.asarray(starts, dtype=np.int64)
+
+
+def autotune(plan: Plan, precision=_lib.PREC_MIXED, reps=3):
+    """Time the translation schemes this plan supports and keep the fastest.
+
+    Candidates: symmetric evaluation on/off, and for the per-direction packed
+    kernel its three block shapes.  Returns {setting: ms}.
+    """
+    results = {}
+    best = None
+    for sym in (1, 0):
+        for shape in ((0,) if sym else (0, 1, 2)):
+            plan.set_option(3, sym)
+            plan.set_option(2, shape)
+            plan.time_translations(precision, reps=1)
+            ms = plan.time_translations(precision, reps=reps)
+            results[(sym, shape)] = ms
+            if best is None or ms < results[best]:
+                best = (sym, shape)
+    plan.set_option(3, best[0])
+    plan.set_option(2, best[1])
+    plan.tuned = best
+    return results
+
+
+class SkelFMMBatch:
+    """Independent instances (points_i, same operator) applied together.
+
+    ``apply(xs)`` takes a list of charge vectors (or one concatenated vector)
+    and returns the list of potentials.  ``capture()`` records the device
+    apply into a CUDA graph for the given precision; later applies replay it.
+    """
+
+    def __init__(self, point_sets, operator, tol=1e-6, leaf_size=128, param=0.0, geometries=None,
+                 npoints_max=500, precision="mixed", tune=True):
+        self.operator = operator
+        self.param = param
+        self.precision = precision
+        self.point_sets = [np.asarray(p, dtype=np.float64) for p in point_sets]
+        self.geometries = geometries
+        self.sizes = [int(p.shape[0]) for p in point_sets]
+        rbs = []
+        for i, pts in enumerate(self.point_sets):
+            tree = BalancedTree(pts, leaf_size)
+            fmm = RecursiveSkeletonization(tree, operator, param, tol,
+                                           geometry=None if geometries is None else geometries[i])
+            fmm.skel_tree(npoints_max=npoints_max)
+            fmm.setup_lists()
+            rbs.append(fmm.ragged())
+        self.instance_ragged = rbs
+        self.ragged, self.starts = concat_ragged(rbs)
+        self.plan = Plan(self.ragged)
+        self.N = int(self.starts[-1])
+        self.cplx = is_complex_op(operator)
+        self._prec = _lib.PREC_MIXED if precision == "mixed" else _lib.PREC_FP64
+        self.tuning = autotune(self.plan, self._prec) if (tune and self._prec != _lib.PREC_FP64) else None
+        dt = torch.complex128 if self.cplx else torch.float64
+        self._x = torch.zeros(self.N, dtype=dt, device="cuda")
+        self._y = torch.zeros(self.N, dtype=dt, device="cuda")
+        self._graph = None
+
+    def capture(self):
+        """Record one device apply (on the internal buffers) into a CUDA graph."""
+        self.plan.apply_device(self._x, self._y, self._prec)  # warm-up outside capture
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        with torch.cuda.graph(g, stream=s):
+            self.plan.apply_device(self._x, self._y, self._prec, torch.cuda.current_stream().cuda_stream)
+        self._graph = g
+        return g
+
+    def apply_device(self, x=None):
+        """Apply to the concatenated device vector ``x`` (or the internal buffer)."""
+        if x is not None:
+            self._x.copy_(x)
+        if self._graph is not None:
+            self._graph.replay()
+        else:
+            self.plan.apply_device(self._x, self._y, self._prec,
+                                   torch.cuda.current_stream().cuda_stream)
+        return self._y
+
+    def apply(self, xs):
+        """Potentials of every instance; ``xs`` is a list of per-instance charge
+        vectors (float32/float64/complex) or one concatenated vector."""
+        x = np.concatenate([np.asarray(v) for v in xs]) if isinstance(xs, (list, tuple)) else np.asarray(xs)
+        if x.shape[0] != self.N:
+            raise ValueError("charge vectors must match the instances' sizes")
+        self._x.copy_(torch.from_numpy(np.ascontiguousarray(x, dtype=np.complex128 if self.cplx else np.float64)))
+        y = self.apply_device().cpu().numpy()
+        return [y[self.starts[i]:self.starts[i + 1]] for i in range(len(self.sizes))]
+
+    def direct_apply(self, i, x, indices):
+        """FP64 direct sum of instance ``i`` at ``indices`` (its own points)."""
+        return direct_sum(self.operator, self.point_sets[i], x, indices, param=self.param,
+                          geometry=None if self.geometries is None else self.geometries[i])
+
+    def relerr(self, xs, ys, ncheck=200, seed=0):
+        """Per-instance relative l-inf error of ``ys`` against the FP64 direct
+        sum on ``ncheck`` sampled targets of each instance."""
+        rng = np.random.default_rng(seed)
+        errs = []
+        for i, (x, y) in enumerate(zip(xs, ys)):
+            idx = rng.choice(self.sizes[i], size=min(ncheck, self.sizes[i]), replace=False)
+            yd = self.direct_apply(i, np.asarray(x, dtype=np.complex128 if self.cplx else np.float64), idx)
+            errs.append(float(np.abs(y[idx] - yd).max() / max(np.abs(yd).max(), 1e-300)))
+        return np.asarray(errs)

@@ -242,6 +242,31 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
     static_assert(kT32Threads * kRowsPerThreadF32 == 256, "mixed work items are 256-row tiles");
     if (p->work32.n > 0) {
       if constexpr (OP == SKF_LAPLACE_2D || OP == SKF_LAPLACE_3D) {
+        if (!p->scalar_mixed && p->sym_ok && p->sym_on) {
+          SymArgs c;
+          c.work_box = p->worksym.box;
+          c.work_row = p->worksym.row;
+          c.box_off = p->box_off;
+          c.box_rank = p->box_rank;
+          c.list_off = p->sym_list_off;
+          c.list_src = p->sym_list_src;
+          c.list_kind = p->sym_list_kind;
+          c.list_poff = p->sym_list_poff;
+          c.box_pbase = p->box_pbase;
+          c.box_pstride = p->box_pstride;
+          c.hi32 = p->hi32;
+          c.lo32 = p->lo32;
+          c.q32 = p->q32;
+          c.qhn32 = p->qhn32;
+          c.qd32 = p->qd32;
+          c.pbuf = p->pbuf;
+          c.u = p->u;
+          c.uh = p->uh;
+          if (p->worksym.n > 0) k_translate_sym<OP><<<p->worksym.n, 128, 0, st>>>(c);
+          k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3((p->max_bs + 255) / 256, p->nboxes), 256, 0, st>>>(
+              p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
+          return;
+        }
         if (!p->scalar_mixed) {
           // packed kernel geometry: warps per block x row pairs per thread
           switch (p->x2_config) {

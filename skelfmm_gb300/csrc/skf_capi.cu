@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <unordered_map>
 #include <vector>
 
 #include "skf_internal.cuh"
@@ -147,6 +148,7 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   p->nperm = d->nperm;
   p->t_len = d->t_len;
   p->nlist = L;
+  for (int b = 0; b < nb; ++b) p->max_bs = std::max<int>(p->max_bs, (int)(d->box_off[b + 1] - d->box_off[b]));
 
   // entry coordinates: FP64 (x,y,z,0) and the FP32 hi/lo split
   std::vector<double4_32a> xyz(E);
@@ -262,6 +264,94 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
     }
   }
 
+  // symmetric translations: every pair (A, B) with A != B is evaluated once,
+  // by the box with the smaller id, when the lists pair each entry with its
+  // mirror (colleague <-> colleague, coarse-up <-> coarse-down, root <-> root)
+  if (d->op == SKF_LAPLACE_2D || d->op == SKF_LAPLACE_3D) {
+    auto mirror = [](int k) {
+      return k == SKF_KIND_COARSE_UP ? SKF_KIND_COARSE_DOWN : (k == SKF_KIND_COARSE_DOWN ? SKF_KIND_COARSE_UP : k);
+    };
+    std::unordered_map<uint64_t, int> seen;
+    seen.reserve((size_t)L * 2);
+    bool ok = true;
+    for (int A = 0; A < nb && ok; ++A)
+      for (int64_t l = d->list_off[A]; l < d->list_off[A + 1]; ++l) {
+        const int B = d->list_src[l];
+        if (B == A) continue;
+        const uint64_t key = (uint64_t)A * (uint64_t)nb + (uint64_t)B;
+        if (seen.count(key)) { ok = false; break; }
+        seen[key] = d->list_kind[l];
+      }
+    for (auto it = seen.begin(); ok && it != seen.end(); ++it) {
+      const uint64_t A = it->first / (uint64_t)nb, B = it->first % (uint64_t)nb;
+      auto m = seen.find(B * (uint64_t)nb + A);
+      if (m == seen.end() || m->second != mirror(it->second)) ok = false;
+    }
+    if (ok) {
+      const int tile = kT32Threads * kRowsPerThreadF32;
+      std::vector<int64_t> soff(nb + 1, 0), poff, pbase(nb, 0), pstride(nb, 0);
+      std::vector<int32_t> ssrc;
+      std::vector<int8_t> skind;
+      std::vector<std::vector<int64_t>> incoming(nb);
+      int64_t total = 0, sym_pairs = 0;
+      std::vector<std::pair<int64_t, std::pair<int32_t, int32_t>>> items;
+      for (int A = 0; A < nb; ++A) {
+        const int64_t bsA = d->box_off[A + 1] - d->box_off[A];
+        const size_t first = ssrc.size();
+        int64_t stride = 0, srcsum = 0;
+        for (int64_t l = d->list_off[A]; l < d->list_off[A + 1]; ++l) {
+          const int B = d->list_src[l];
+          if (B < A) continue;
+          const int64_t bsB = d->box_off[B + 1] - d->box_off[B];
+          ssrc.push_back(B);
+          skind.push_back(d->list_kind[l]);
+          poff.push_back(B == A ? 0 : stride);
+          if (B != A) stride += 2 * bsB;
+          srcsum += bsB;
+        }
+        soff[A + 1] = (int64_t)ssrc.size();
+        pstride[A] = stride;
+        pbase[A] = total;
+        const int64_t ntiles = bsA > 0 ? (bsA + tile - 1) / tile : 0;
+        for (int64_t t = 0; t < ntiles; ++t)
+          for (size_t k = first; k < ssrc.size(); ++k)
+            if (ssrc[k] != A) incoming[ssrc[k]].push_back(total + t * stride + poff[k]);
+        total += ntiles * stride;
+        sym_pairs += bsA * srcsum;
+        if (bsA > 0 && ssrc.size() > first)
+          for (int r0 = 0; r0 < bsA; r0 += tile)
+            items.push_back({std::min<int64_t>(tile, bsA - r0) * srcsum, {A, r0}});
+      }
+      std::stable_sort(items.begin(), items.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+      std::vector<int32_t> wb(items.size()), wr(items.size());
+      for (size_t i = 0; i < items.size(); ++i) {
+        wb[i] = items[i].second.first;
+        wr[i] = items[i].second.second;
+      }
+      std::vector<int64_t> ioff(nb + 1, 0), iblk;
+      for (int B = 0; B < nb; ++B) {
+        ioff[B + 1] = ioff[B] + (int64_t)incoming[B].size();
+        iblk.insert(iblk.end(), incoming[B].begin(), incoming[B].end());
+      }
+      SKF_TRY(upload(p, &p->sym_list_off, soff.data(), soff.size()));
+      SKF_TRY(upload(p, &p->sym_list_src, ssrc.data(), std::max<size_t>(ssrc.size(), 1)));
+      SKF_TRY(upload(p, &p->sym_list_kind, skind.data(), std::max<size_t>(skind.size(), 1)));
+      SKF_TRY(upload(p, &p->sym_list_poff, poff.data(), std::max<size_t>(poff.size(), 1)));
+      SKF_TRY(upload(p, &p->box_pbase, pbase.data(), pbase.size()));
+      SKF_TRY(upload(p, &p->box_pstride, pstride.data(), pstride.size()));
+      SKF_TRY(upload(p, &p->in_off, ioff.data(), ioff.size()));
+      if (!iblk.empty()) SKF_TRY(upload(p, &p->in_blk, iblk.data(), iblk.size()));
+      SKF_TRY(upload(p, &p->pbuf, (const float*)nullptr, (size_t)std::max<int64_t>(total, 1)));
+      p->worksym.n = (int)items.size();
+      if (p->worksym.n > 0) {
+        SKF_TRY(upload(p, &p->worksym.box, wb.data(), wb.size()));
+        SKF_TRY(upload(p, &p->worksym.row, wr.data(), wr.size()));
+      }
+      p->sym_pairs = sym_pairs;
+      p->sym_ok = true;
+    }
+  }
+
   SKF_TRY(upload(p, &p->q, (const double*)nullptr, (size_t)E * W));
   SKF_TRY(upload(p, &p->qh, (const double*)nullptr, (size_t)E * W));
   SKF_TRY(upload(p, &p->u, (const double*)nullptr, (size_t)E * W));
@@ -300,6 +390,7 @@ int skf_plan_query(const skf_plan* p, skf_plan_info* info) {
   info->device_bytes = p->device_bytes;
   info->nwork = p->work32.n;
   info->is_complex = p->cplx ? 1 : 0;
+  info->npairs_evaluated_mixed = (p->sym_ok && p->sym_on && !p->scalar_mixed) ? p->sym_pairs : p->pairs;
   return SKF_OK;
 }
 
@@ -332,6 +423,7 @@ int skf_plan_set_option(skf_plan* p, int32_t option, int64_t value) {
   if (!p) return SKF_ERR_ARG;
   switch (option) {
     case SKF_OPT_SCALAR_MIXED: p->scalar_mixed = value != 0; return SKF_OK;
+    case SKF_OPT_SYMMETRIC: p->sym_on = value != 0; return SKF_OK;
     case SKF_OPT_PACKED_SHAPE:
       if (value < 0 || value > 2) return SKF_ERR_ARG;
       p->x2_config = (int)value;

@@ -51,6 +51,20 @@ struct skf_plan {
   bool cplx = false;
   bool scalar_mixed = false;  // force the scalar FP32 translation kernel (comparison/testing)
   int x2_config = 0;          // packed kernel: 0 = 4 warps x 1 pair, 1 = 1 x 4, 2 = 2 x 2
+  // symmetric translations (mixed path, symmetric point kernels, symmetric lists)
+  bool sym_ok = false;  // usable for this plan
+  bool sym_on = true;   // option SKF_OPT_SYMMETRIC
+  int64_t* sym_list_off = nullptr;
+  int32_t* sym_list_src = nullptr;
+  int8_t* sym_list_kind = nullptr;
+  int64_t* sym_list_poff = nullptr;
+  int64_t* box_pbase = nullptr;
+  int64_t* box_pstride = nullptr;
+  int64_t* in_off = nullptr;
+  int64_t* in_blk = nullptr;
+  float* pbuf = nullptr;
+  int64_t sym_pairs = 0;  // kernel evaluations per apply on the symmetric path
+  int max_bs = 0;         // largest box
   double kappa = 0.0;
   int64_t E = 0, N = 0, nperm = 0, t_len = 0, nlist = 0;
   int64_t pairs = 0;  // kernel evaluations per apply
@@ -76,7 +90,7 @@ struct skf_plan {
   int64_t* list_off = nullptr;
   int32_t* list_src = nullptr;
   int8_t* list_kind = nullptr;
-  skf::WorkList work64, work32;
+  skf::WorkList work64, work32, worksym;
   std::vector<skf::LevelBoxes> levels;  // indexed by level
   // apply vectors (scalars; complex: 2 doubles per entry)
   double* q = nullptr;

@@ -566,3 +566,322 @@ __global__ void __launch_bounds__(NW * 32) k_translate_f32x2(TransArgs32 a) {
 }
 
 }  // namespace skf
+
+namespace skf {
+
+// ------------------------------------------------------------------ symmetric (mixed, packed)
+// Symmetric point kernels (K(x,y) = K(y,x)) and symmetric lists: every
+// translation (A <- B, kind k) has a mirror (B <- A, mirror kind:
+// colleague <-> colleague, coarse-up <-> coarse-down, root <-> root) that uses
+// the same kernel block transposed.  Box A owns its pairs with B > A: one
+// evaluation of K(X_A, X_B) feeds both
+//   rows of A:    u_A[i] += sum_j K_ij c1_j(k),   uh_A[i] += sum_j K_ij c2_j(k)
+//   rows of B:    u_B[j] += sum_i K_ij c1_i(k'),  uh_B[j] += sum_i K_ij c2_i(k')
+// The B-side sums of one work item (its 256 rows of A) go to a partial buffer
+// (fixed slot per item, list entry and source), and k_sym_reduce adds them in
+// a fixed order: deterministic, no atomics.  Self pairs are evaluated once as
+// before.
+//
+// Lane layout per warp (64 rows of A): lane = 8 ls + lr; lane (lr, ls) owns
+// rows wrow0 + lr + 8k (k < 8, packed in pairs k = 2p, 2p+1) and the sources
+// j = t0 + ls + 4g of each tile.  Row sums are combined across the 4 ls lanes
+// at the end; a source's B-side sum is combined across the 8 lr lanes with 3
+// shuffles, then across the 4 warps through shared memory.
+struct SymArgs {
+  const int32_t* work_box;
+  const int32_t* work_row;
+  const int64_t* box_off;
+  const int32_t* box_rank;
+  const int64_t* list_off;   // symmetric lists: self + owned entries
+  const int32_t* list_src;
+  const int8_t* list_kind;
+  const int64_t* list_poff;  // offset of the entry's partial block within a tile region
+  const int64_t* box_pbase;  // first partial of the box's tile regions
+  const int64_t* box_pstride;  // partials per tile region of the box
+  const float4* hi32;
+  const float4* lo32;
+  const float* q32;
+  const float* qhn32;
+  const float* qd32;
+  float* pbuf;
+  double* u;
+  double* uh;
+};
+
+constexpr int kSymPairs = 2;  // packed row pairs per lane (4 rows)
+constexpr int kSymTS = 64;    // sources per shared-memory tile
+constexpr int kSymLd = kSymTS + 2;  // row stride = 2 (mod 32): lanes (lr, ls) write distinct banks
+
+// One tile: lane (lr, ls) evaluates its 4 rows against sources j = 2g + ls.
+// Row sums accumulate in registers; the lane's B-side sum for source j (its 4
+// rows) goes to sTu[lr][j] / sTh[lr][j] and is reduced after the tile.
+template <int D, bool HR, bool HT, bool TR, bool SELF, bool LOG>
+__device__ __forceinline__ void sym_tile(const ulonglong2* __restrict__ s0, const ulonglong2* __restrict__ s1,
+                                         const ulonglong2* __restrict__ s2, const ulonglong2* __restrict__ s3,
+                                         int nt, int ls, int lr, const f2_t (&thx)[kSymPairs],
+                                         const f2_t (&thy)[kSymPairs], const f2_t (&thz)[kSymPairs],
+                                         const f2_t (&tlx)[kSymPairs], const f2_t (&tly)[kSymPairs],
+                                         const f2_t (&tlz)[kSymPairs], const f2_t (&c1T)[kSymPairs],
+                                         const f2_t (&c2T)[kSymPairs], f2_t (&pu)[kSymPairs],
+                                         f2_t (&ph)[kSymPairs], float (*__restrict__ sTu)[kSymLd],
+                                         float (*__restrict__ sTh)[kSymLd]) {
+#pragma unroll 4
+  for (int j = ls; j < nt; j += 2) {
+    const ulonglong2 A = s0[j];   // (-hx,-hx), (-hy,-hy)
+    const ulonglong2 B = s1[j];   // (-hz,-hz), (-lx,-lx)
+    const ulonglong2 Cc = s2[j];  // (-ly,-ly), (-lz,-lz)
+    const ulonglong2 Q = s3[j];   // (c1,c1), (c2,c2)
+    f2_t tu = 0ull, th = 0ull;
+#pragma unroll
+    for (int p = 0; p < kSymPairs; ++p) {
+      const f2_t dx = f2_add(f2_add(thx[p], A.x), f2_add(tlx[p], B.y));
+      const f2_t dy = f2_add(f2_add(thy[p], A.y), f2_add(tly[p], Cc.x));
+      f2_t r2 = f2_mul(dx, dx);
+      r2 = f2_fma(dy, dy, r2);
+      if (D == 3) {
+        const f2_t dz = f2_add(f2_add(thz[p], B.x), f2_add(tlz[p], Cc.y));
+        r2 = f2_fma(dz, dz, r2);
+      }
+      float ra, rb;
+      f2_unpack(r2, ra, rb);
+      float ka = LOG ? lg2_approx(ra) : rsqrt_approx(ra);
+      float kb = LOG ? lg2_approx(rb) : rsqrt_approx(rb);
+      if (SELF) {
+        ka = ra > 0.f ? ka : 0.f;
+        kb = rb > 0.f ? kb : 0.f;
+      }
+      const f2_t k = f2_pack(ka, kb);
+      pu[p] = f2_fma(k, Q.x, pu[p]);
+      if (HR) ph[p] = f2_fma(k, Q.y, ph[p]);
+      if (TR) {
+        tu = p == 0 ? f2_mul(k, c1T[p]) : f2_fma(k, c1T[p], tu);
+        if (HT) th = p == 0 ? f2_mul(k, c2T[p]) : f2_fma(k, c2T[p], th);
+      }
+    }
+    if (TR) {
+      float a, b;
+      f2_unpack(tu, a, b);
+      sTu[lr][j] = a + b;
+      if (HT) {
+        f2_unpack(th, a, b);
+        sTh[lr][j] = a + b;
+      }
+    }
+  }
+}
+
+template <int OP>
+__global__ void __launch_bounds__(128, 5) k_translate_sym(SymArgs a) {
+  constexpr int D = OpTraits<OP>::kDim;
+  constexpr bool LOG = (OP == SKF_LAPLACE_2D);
+  constexpr int TS = kSymTS;
+  constexpr int NW = 4;
+  __shared__ ulonglong2 s0[TS], s1[TS], s2[TS], s3[TS];
+  __shared__ float sTu[NW][16][kSymLd];
+  __shared__ float sTh[NW][16][kSymLd];
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lr = lane & 15, ls = lane >> 4;
+  const int U = a.work_box[blockIdx.x];
+  const int row0 = a.work_row[blockIdx.x];
+  const int64_t offU = a.box_off[U];
+  const int bsU = (int)(a.box_off[U + 1] - offU);
+  const int rU = a.box_rank[U];
+  const int wrow0 = row0 + 64 * warp;
+  const bool active = wrow0 < bsU;
+  const int64_t pbase = a.box_pbase[U] + (int64_t)(row0 / 256) * a.box_pstride[U];
+
+  // rows of this lane: wrow0 + lr + 16 k, k < 4, packed pairs (0,1), (2,3)
+  f2_t thx[kSymPairs], thy[kSymPairs], thz[kSymPairs], tlx[kSymPairs], tly[kSymPairs], tlz[kSymPairs];
+#pragma unroll
+  for (int p = 0; p < kSymPairs; ++p) {
+    const int ra = wrow0 + lr + 32 * p, rb = ra + 16;
+    const int64_t ea = offU + max(0, min(ra, bsU - 1)), eb = offU + max(0, min(rb, bsU - 1));
+    const float4 ha = a.hi32[ea], hb = a.hi32[eb];
+    const float4 la = a.lo32[ea], lb = a.lo32[eb];
+    thx[p] = f2_pack(ha.x, hb.x);
+    thy[p] = f2_pack(ha.y, hb.y);
+    thz[p] = f2_pack(ha.z, hb.z);
+    tlx[p] = f2_pack(la.x, lb.x);
+    tly[p] = f2_pack(la.y, lb.y);
+    tlz[p] = f2_pack(la.z, lb.z);
+  }
+  const bool skel_rows = wrow0 < rU;
+  const f2_t zero = 0ull;
+  f2_t su[kSymPairs], cu[kSymPairs], sh[kSymPairs], ch[kSymPairs];
+#pragma unroll
+  for (int p = 0; p < kSymPairs; ++p) su[p] = cu[p] = sh[p] = ch[p] = zero;
+
+  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
+  for (int64_t l = l0; l < l1; ++l) {
+    const int s = a.list_src[l];
+    const int kind = a.list_kind[l];
+    const int64_t offS = a.box_off[s];
+    const int bsS = (int)(a.box_off[s + 1] - offS);
+    const int rS = a.box_rank[s];
+    const bool self = (s == U);
+    const int nh = (kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_DOWN)
+                       ? rS
+                       : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
+    const float* c1src = (kind == SKF_KIND_COARSE_DOWN) ? a.qd32 : a.q32;
+    // charges of A's rows seen from B (mirror kind), for the B-side sums
+    f2_t c1T[kSymPairs], c2T[kSymPairs];
+#pragma unroll
+    for (int p = 0; p < kSymPairs; ++p) c1T[p] = c2T[p] = zero;
+    if (!self) {
+      const float* t1 = (kind == SKF_KIND_COARSE_UP) ? a.qd32 : a.q32;
+#pragma unroll
+      for (int p = 0; p < kSymPairs; ++p) {
+        const int ra = wrow0 + lr + 32 * p, rb = ra + 16;
+        const float ca = ra < bsU ? t1[offU + ra] : 0.f, cb = rb < bsU ? t1[offU + rb] : 0.f;
+        c1T[p] = f2_pack(ca, cb);
+        float da = 0.f, db = 0.f;
+        if (kind == SKF_KIND_COLLEAGUE) {
+          da = ra < bsU ? a.qhn32[offU + ra] : 0.f;
+          db = rb < bsU ? a.qhn32[offU + rb] : 0.f;
+        } else if (kind == SKF_KIND_COARSE_DOWN) {
+          da = -ca;
+          db = -cb;
+        }
+        c2T[p] = f2_pack(da, db);
+      }
+    }
+    const bool row_h_kind = kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_UP;
+    const bool t_h_kind = kind == SKF_KIND_COLLEAGUE ? skel_rows : kind == SKF_KIND_COARSE_DOWN;
+    const int64_t pblk = self ? 0 : pbase + a.list_poff[l];
+    for (int t0 = 0; t0 < bsS;) {
+      const bool hseg = t0 < nh;
+      const int nt = min(TS, (hseg ? nh : bsS) - t0);
+      __syncthreads();
+      for (int j = threadIdx.x; j < nt; j += NW * 32) {
+        const int64_t e = offS + t0 + j;
+        const float4 h = a.hi32[e], lo = a.lo32[e];
+        const float c1 = c1src[e];
+        float c2 = 0.f;
+        if (kind == SKF_KIND_COLLEAGUE) c2 = a.qhn32[e];
+        else if (kind == SKF_KIND_COARSE_UP) c2 = -c1;
+        s0[j] = make_ulonglong2(f2_pack(-h.x, -h.x), f2_pack(-h.y, -h.y));
+        s1[j] = make_ulonglong2(f2_pack(-h.z, -h.z), f2_pack(-lo.x, -lo.x));
+        s2[j] = make_ulonglong2(f2_pack(-lo.y, -lo.y), f2_pack(-lo.z, -lo.z));
+        s3[j] = make_ulonglong2(f2_pack(c1, c1), f2_pack(c2, c2));
+      }
+      __syncthreads();
+      const bool hr = active && hseg && row_h_kind && skel_rows;
+      const bool ht = active && hseg && t_h_kind;
+      f2_t pu[kSymPairs], ph[kSymPairs];
+#pragma unroll
+      for (int p = 0; p < kSymPairs; ++p) pu[p] = ph[p] = zero;
+      float(*tu)[kSymLd] = sTu[warp];
+      float(*thp)[kSymLd] = sTh[warp];
+      if (active) {
+        if (self) {
+          if (hr) sym_tile<D, true, false, false, true, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          else sym_tile<D, false, false, false, true, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+        } else if (hr) {
+          if (ht) sym_tile<D, true, true, true, false, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          else sym_tile<D, true, false, true, false, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+        } else {
+          if (ht) sym_tile<D, false, true, true, false, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          else sym_tile<D, false, false, true, false, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+        }
+#pragma unroll
+        for (int p = 0; p < kSymPairs; ++p) {
+          f2_two_sum(su[p], cu[p], pu[p]);
+          if (hr) f2_two_sum(sh[p], ch[p], ph[p]);
+        }
+      }
+      if (!self) {
+        // warps without rows, or without a B-side uh sum, contribute zeros
+        if (!active || !ht) {
+          for (int k = lane; k < 16 * TS; k += 32) {
+            const int rr = k / TS, jj = k - rr * TS;
+            if (jj < nt) {
+              if (!active) tu[rr][jj] = 0.f;
+              thp[rr][jj] = 0.f;
+            }
+          }
+        }
+        __syncthreads();
+        // threads 0..63 add the u partials of source j = tid, threads 64..127
+        // the uh partials: 4 warps x 16 lanes each, consecutive j per thread
+        const int j = threadIdx.x & (TS - 1);
+        const bool hpart = threadIdx.x >= TS;
+        if (j < nt) {
+          float (*src)[16][kSymLd] = hpart ? sTh : sTu;
+          float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
+#pragma unroll
+          for (int r = 0; r < 16; ++r) {
+            v0 += src[0][r][j];
+            v1 += src[1][r][j];
+            v2 += src[2][r][j];
+            v3 += src[3][r][j];
+          }
+          a.pbuf[pblk + (hpart ? bsS : 0) + t0 + j] = (v0 + v1) + (v2 + v3);
+        }
+      }
+      t0 += nt;
+    }
+  }
+  // combine the row sums of the 2 lanes sharing rows (ls = 0, 1), in FP64
+#pragma unroll
+  for (int p = 0; p < kSymPairs; ++p) {
+    float sua, sub, cua, cub, sha, shb, cha, chb;
+    f2_unpack(su[p], sua, sub);
+    f2_unpack(cu[p], cua, cub);
+    f2_unpack(sh[p], sha, shb);
+    f2_unpack(ch[p], cha, chb);
+    double v[4] = {(double)sua + (double)cua, (double)sub + (double)cub, (double)sha + (double)cha,
+                   (double)shb + (double)chb};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], 16);
+    if (active && ls == 0) {
+      const double scale = LOG ? 0.34657359027997264 : 1.0;
+      const int ra = wrow0 + lr + 32 * p, rb = ra + 16;
+      if (ra < bsU) {
+        a.u[offU + ra] = scale * v[0];
+        a.uh[offU + ra] = ra < rU ? scale * v[2] : 0.0;
+      }
+      if (rb < bsU) {
+        a.u[offU + rb] = scale * v[1];
+        a.uh[offU + rb] = rb < rU ? scale * v[3] : 0.0;
+      }
+    }
+  }
+}
+
+// Adds the B-side partial sums into u / uh in a fixed order.  Block
+// (chunk, box): entries [256 chunk, 256 chunk + 256) of the box.
+template <bool LOG>
+__global__ void __launch_bounds__(256) k_sym_reduce(const int64_t* __restrict__ box_off,
+                                                    const int32_t* __restrict__ box_rank,
+                                                    const int64_t* __restrict__ in_off,
+                                                    const int64_t* __restrict__ in_blk,
+                                                    const float* __restrict__ pbuf, double* __restrict__ u,
+                                                    double* __restrict__ uh) {
+  const int B = blockIdx.y;
+  const int64_t off = box_off[B];
+  const int bs = (int)(box_off[B + 1] - off);
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k0 = in_off[B], k1 = in_off[B + 1];
+  if (j >= bs || k0 == k1) return;
+  const int r = box_rank[B];
+  const double scale = LOG ? 0.34657359027997264 : 1.0;
+  double su0 = 0.0, su1 = 0.0, sh0 = 0.0, sh1 = 0.0;
+  int64_t k = k0;
+  for (; k + 1 < k1; k += 2) {
+    const int64_t b0 = in_blk[k], b1 = in_blk[k + 1];
+    su0 += (double)pbuf[b0 + j];
+    su1 += (double)pbuf[b1 + j];
+    sh0 += (double)pbuf[b0 + bs + j];
+    sh1 += (double)pbuf[b1 + bs + j];
+  }
+  if (k < k1) {
+    const int64_t b0 = in_blk[k];
+    su0 += (double)pbuf[b0 + j];
+    sh0 += (double)pbuf[b0 + bs + j];
+  }
+  u[off + j] += scale * (su0 + su1);
+  if (j < r) uh[off + j] += scale * (sh0 + sh1);
+}
+
+}  // namespace skf

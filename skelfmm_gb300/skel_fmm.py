@@ -37,6 +37,49 @@ def warmup_cuda_fmm_apply(apply, x):
     return True
 
 
+def direct_sum(operator, points, x, indices, *, param=0.0, geometry=None, device=None):
+    """FP64 direct sum ``(K x)[indices]`` over all ``points`` on the GPU.
+
+    The kernel is evaluated on the fly (``skf_kernel_apply``); a coincident
+    pair contributes 0, as in the dense kernels.
+    """
+    from .kernels import batched_kernel_apply
+
+    dev = torch.device("cuda") if device is None else device
+    points = np.asarray(points, dtype=np.float64)
+    idx = np.asarray(indices, dtype=np.int64)
+    cplx = is_complex_op(operator)
+    n = points.shape[0]
+    # sources split into chunks, one batched "pair" per chunk, so the sum
+    # spreads over the whole GPU; partial sums are added in FP64
+    nchunk = max(1, min(1024, n // 4096))
+    csz = -(-n // nchunk)
+    pad = nchunk * csz - n
+    pts = np.concatenate((points, np.zeros((pad, points.shape[1]))))
+    xv = np.concatenate((np.asarray(x, dtype=np.complex128 if cplx else np.float64),
+                         np.zeros(pad, dtype=np.complex128 if cplx else np.float64)))
+    src = torch.from_numpy(pts.reshape(nchunk, csz, -1)).to(dev)
+    xq = torch.from_numpy(xv.reshape(nchunk, csz, 1)).to(dev)
+    ncnt = torch.full((nchunk,), csz, dtype=torch.int32, device=dev)
+    ncnt[-1] = csz - pad
+    gs = None
+    if operator.geometry_side == "source":
+        g = np.concatenate((geometry, np.zeros((pad, 3))))
+        gs = torch.from_numpy(np.ascontiguousarray(g, dtype=np.float64).reshape(nchunk, csz, 3)).to(dev)
+    out = []
+    for s in range(0, idx.shape[0], 2048):
+        t = idx[s: s + 2048]
+        trg = torch.from_numpy(np.ascontiguousarray(points[t])).to(dev).unsqueeze(0).expand(nchunk, -1, -1)
+        gtt = None
+        if operator.geometry_side == "target":
+            gtt = torch.from_numpy(np.ascontiguousarray(geometry[t], dtype=np.float64)).to(dev)
+            gtt = gtt.unsqueeze(0).expand(nchunk, -1, -1)
+        part = batched_kernel_apply(cuda_op_id(operator), xq, trg, src, param=param, geom_trg=gtt,
+                                    geom_src=gs, n=ncnt)
+        out.append(part.sum(dim=0)[:, 0].cpu().numpy())
+    return np.concatenate(out)
+
+
 class SkelFMM:
     """Build and apply a fast operator on one GPU."""
 
@@ -182,41 +225,8 @@ class SkelFMM:
 
     def direct_apply(self, x, indices):
         """FP64 direct sum ``(K x)[indices]`` on the GPU (kernel evaluated on the fly)."""
-        from .kernels import batched_kernel_apply
-
-        idx = np.asarray(indices, dtype=np.int64)
-        cplx = is_complex_op(self.operator)
-        dev = self.device
-        n = self.points.shape[0]
-        # sources split into chunks, one batched "pair" per chunk, so the sum
-        # spreads over the whole GPU; partial sums are added in FP64
-        nchunk = max(1, min(1024, n // 4096))
-        csz = -(-n // nchunk)
-        pad = nchunk * csz - n
-        pts = np.concatenate((self.points, np.zeros((pad, self.points.shape[1]))))
-        xv = np.concatenate((np.asarray(x, dtype=np.complex128 if cplx else np.float64),
-                             np.zeros(pad, dtype=np.complex128 if cplx else np.float64)))
-        src = torch.from_numpy(pts.reshape(nchunk, csz, -1)).to(dev)
-        xq = torch.from_numpy(xv.reshape(nchunk, csz, 1)).to(dev)
-        ncnt = torch.full((nchunk,), csz, dtype=torch.int32, device=dev)
-        ncnt[-1] = csz - pad
-        gs = None
-        if self.operator.geometry_side == "source":
-            g = np.concatenate((self.geometry, np.zeros((pad, 3))))
-            gs = torch.from_numpy(np.ascontiguousarray(g, dtype=np.float64).reshape(nchunk, csz, 3)).to(dev)
-        out = []
-        for s in range(0, idx.shape[0], 2048):
-            t = idx[s: s + 2048]
-            trg = torch.from_numpy(np.ascontiguousarray(self.points[t])).to(dev).unsqueeze(0).expand(nchunk, -1, -1)
-            gtt = None
-            if self.operator.geometry_side == "target":
-                gtt = torch.from_numpy(np.ascontiguousarray(self.geometry[t], dtype=np.float64)).to(dev)
-                gtt = gtt.unsqueeze(0).expand(nchunk, -1, -1)
-            # a coincident pair contributes 0, as in the dense kernels
-            part = batched_kernel_apply(cuda_op_id(self.operator), xq, trg, src, param=self.param, geom_trg=gtt,
-                                        geom_src=gs, n=ncnt)
-            out.append(part.sum(dim=0)[:, 0].cpu().numpy())
-        return np.concatenate(out)
+        return direct_sum(self.operator, self.points, x, indices, param=self.param, geometry=self.geometry,
+                          device=self.device)
 
     def relerr_fmm_apply_check(self, x, *, ncheck=64, seed=0, indices=None):
         """||y_dense - y_fmm||_inf / ||y_dense||_inf on a subset of targets (skel_fmm.py:218-257).
