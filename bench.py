@@ -255,26 +255,35 @@ def run_ours(args):
     err_mixed = float(np.abs(ymix[idx] - yd).max() / den)
     err_fp64 = None if y64 is None else float(np.abs(y64[idx] - yd).max() / den)
 
-    # roofline of the dominant kernel (translations, mixed): algorithmic kernel
-    # pair evaluations per launch (counted from the built lists) over the
-    # launch's device time.  Per pair the algorithm needs 7 FP32 FMA-pipe ops
-    # (3 sub, 3 FMA for r^2, 1 FMA accumulate) and 1 rsqrt on the XU pipe.
-    # GB300: 128 FMA-pipe lanes/clk/SM; the XU pipe issues 32 lanes/clk/SM
-    # (ncu pct_of_peak of sm__inst_executed_pipe_xu), so the FMA pipe binds:
-    # peak = 152 SMs x 128/7 pairs/clk x max SM clock.
+    # roofline of the dominant stage (translations, mixed).  Units are kernel
+    # evaluations counted from the built lists.  Per evaluation the algorithm
+    # needs 3 FP32 subtractions, 3 FMA-pipe ops for r^2, 1 rsqrt (XU pipe) and
+    # one FMA per direction it feeds: 7 FMA-pipe ops on the per-direction
+    # path, 8 on the symmetric path (one evaluation feeds both directions).
+    # GB300: 128 FMA-pipe lanes/clk/SM; the XU pipe (32 lanes/clk/SM by ncu
+    # pct_of_peak of sm__inst_executed_pipe_xu) is not binding.
+    # peak = 152 SMs x 128/ops evaluations/clk x max SM clock.  The timed
+    # launch covers the whole translation stage (on the symmetric path the
+    # evaluation kernel plus the partial-sum reduction).
     peaks, src = measured_peaks()
     t_ms = plan.time_translations(_lib.PREC_MIXED, reps=5, stream=sp)
-    pairs = int(plan.info.npairs_fused)
-    achieved = pairs / (t_ms * 1e-3) / 1e9
+    info = plan.info
+    pairs = int(info.npairs_fused)
+    evals = int(info.npairs_evaluated_mixed)
+    sym = evals < pairs
+    ops = 8 if sym else 7
+    achieved = evals / (t_ms * 1e-3) / 1e9
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    peak = 152 * (128.0 / 7.0) * sm_mhz * 1e6 / 1e9
+    peak = 152 * (128.0 / ops) * sm_mhz * 1e6 / 1e9
+    kern = "k_translate_sym<LAPLACE_3D> + k_sym_reduce" if sym else "k_translate_f32x2<LAPLACE_3D>"
     roofline = {
-        "bound": "fp32-fma", "kernel": "k_translate_f32x2<LAPLACE_3D>", "achieved": round(achieved, 1),
-        "peak": round(peak, 1), "unit": "Gpair/s", "frac": round(achieved / peak, 4),
-        "traffic": profiled_traffic("translate_lap3d_1M.md"),
-        "peak_source": f"152 SMs x 128/7 pairs/clk (FP32 FMA pipe, 7 ops/pair) x sm_max_mhz {sm_mhz:.0f} "
-                       f"({src} MEASURED_PEAKS.json clock); XU (rsqrt) 32/clk/SM is not binding",
-        "pairs_per_launch": pairs, "launch_ms": round(t_ms, 4),
+        "bound": "fp32-fma", "kernel": kern, "achieved": round(achieved, 1),
+        "peak": round(peak, 1), "unit": "Geval/s", "frac": round(achieved / peak, 4),
+        "traffic": profiled_traffic("translate_sym_lap3d_1M.md" if sym else "translate_lap3d_1M.md"),
+        "peak_source": f"152 SMs x 128/{ops} evaluations/clk (FP32 FMA pipe, {ops} ops per evaluation) x "
+                       f"sm_max_mhz {sm_mhz:.0f} ({src} MEASURED_PEAKS.json clock); XU (rsqrt) not binding",
+        "evaluations_per_launch": evals, "pairs_per_launch": pairs, "launch_ms": round(t_ms, 4),
+        "pairs_per_s_G": round(pairs / (t_ms * 1e-3) / 1e9, 1),
     }
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -291,7 +300,7 @@ def run_ours(args):
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": round(n * ws / e2e_s / 1e6, 2), "unit": "Mpts/s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8, "ms_per_step": round(e2e_s * 1e3, 3)},
-        "gpu_launches": launches_per_apply(plan),
+        "gpu_launches": int(info.launches_mixed) * args.steps,
         "build_s": round(build_s, 3),
         "fp64_ms_per_step": None if ms_fp64 is None else round(ms_fp64, 3),
         "mixed_over_fp64": None if ms_fp64 is None else round(ms_fp64 / ms_step, 2),
@@ -304,15 +313,6 @@ def run_ours(args):
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
-
-
-def launches_per_apply(plan):
-    rb = plan.rb
-    lv = rb.box_level
-    rk = rb.box_rank
-    levels = sum(1 for L in range(rb.root_level + 1, rb.nlevels) if np.any((lv == L) & (rk > 0)))
-    # permute in/out + up/down per level + one translation launch (memsets excluded)
-    return 2 + 2 * levels + 1
 
 
 def run_reference(args):
@@ -331,7 +331,20 @@ def run_reference(args):
     ncores = os.cpu_count() or 1
     t0 = time.perf_counter()
     tree = BalancedTree(pts, args.leaf)
-    with ctx.Pool(ncores) as pool:
+    # one BLAS thread per pool worker (the workers read these at import; a
+    # multi-threaded BLAS in every worker oversubscribes the cores)
+    blas_env = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in blas_env}
+    os.environ.update({k: "1" for k in blas_env})
+    try:
+        pool = ctx.Pool(ncores)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    with pool:
         ob = O.OracleBuild(tree, O.OPERATORS["laplace_3d"], 0.0, args.tol).skel_tree(500, pool=pool)
     build_s = time.perf_counter() - t0
     oa = O.OracleApply(ob, nthreads=ncores)

@@ -99,6 +99,8 @@ typedef struct {
   int32_t is_complex;
   int64_t npairs_evaluated_mixed; /* kernel evaluations the mixed apply performs
                                      (fewer than npairs_fused on the symmetric path) */
+  int32_t launches_fp64;  /* kernel launches of one FP64 apply (memsets excluded) */
+  int32_t launches_mixed; /* kernel launches of one mixed apply (memsets excluded) */
 } skf_plan_info;
 
 int skf_plan_create(const skf_plan_desc* desc, skf_plan** out);

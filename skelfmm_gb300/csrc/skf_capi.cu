@@ -390,7 +390,12 @@ int skf_plan_query(const skf_plan* p, skf_plan_info* info) {
   info->device_bytes = p->device_bytes;
   info->nwork = p->work32.n;
   info->is_complex = p->cplx ? 1 : 0;
-  info->npairs_evaluated_mixed = (p->sym_ok && p->sym_on && !p->scalar_mixed) ? p->sym_pairs : p->pairs;
+  const bool sym = p->sym_ok && p->sym_on && !p->scalar_mixed;
+  info->npairs_evaluated_mixed = sym ? p->sym_pairs : p->pairs;
+  int lv = 0;
+  for (int l = p->root_level + 1; l < p->nlevels; ++l) lv += p->levels[l].n > 0 ? 1 : 0;
+  info->launches_fp64 = 2 + 2 * lv + (p->work64.n > 0 ? 1 : 0);
+  info->launches_mixed = 2 + 2 * lv + 1 + (sym ? (p->worksym.n > 0 ? 1 : 0) + 1 : (p->work32.n > 0 ? 1 : 0));
   return SKF_OK;
 }
 
