@@ -39,11 +39,24 @@ _MAX_DEPTH = {2: 30, 3: 20}
 
 
 def _spread_bits(v: np.ndarray, ndim: int, nbits: int) -> np.ndarray:
-    out = np.zeros(v.shape, dtype=np.uint64)
-    one = np.uint64(1)
-    for b in range(nbits):
-        out |= ((v >> np.uint64(b)) & one) << np.uint64(b * ndim)
-    return out
+    """Put bit b of ``v`` at bit b*ndim (the standard shift-and-mask bit
+    interleave; 2D up to 32 bits, 3D up to 21 bits)."""
+    x = v.astype(np.uint64) & np.uint64((1 << nbits) - 1 if nbits < 64 else ~0)
+    if ndim == 2:
+        steps = ((16, 0x0000FFFF0000FFFF), (8, 0x00FF00FF00FF00FF), (4, 0x0F0F0F0F0F0F0F0F),
+                 (2, 0x3333333333333333), (1, 0x5555555555555555))
+    elif ndim == 3:
+        steps = ((32, 0x001F00000000FFFF), (16, 0x001F0000FF0000FF), (8, 0x100F00F00F00F00F),
+                 (4, 0x10C30C30C30C30C3), (2, 0x1249249249249249))
+    else:
+        out = np.zeros(v.shape, dtype=np.uint64)
+        one = np.uint64(1)
+        for bit in range(nbits):
+            out |= ((x >> np.uint64(bit)) & one) << np.uint64(bit * ndim)
+        return out
+    for sh, mask in steps:
+        x = (x | (x << np.uint64(sh))) & np.uint64(mask)
+    return x
 
 
 def morton_encode(coords: np.ndarray, nbits: int) -> np.ndarray:
@@ -101,18 +114,20 @@ class BalancedTree:
         self._skeys = keys[perm]
         self._sq = q[perm]
 
-        # per level: dict coords-tuple -> [start, end, is_leaf]
-        levels = [{(0,) * ndim: [0, self.N, True]}]
-        self._levels = levels
+        # per level (sorted by Morton code): coords, codes, point ranges, leaf flags
+        self._Lc = [np.zeros((1, ndim), dtype=np.int64)]
+        self._Lk = [np.zeros(1, dtype=np.uint64)]
+        self._Ls = [np.zeros(1, dtype=np.int64)]
+        self._Le = [np.full(1, self.N, dtype=np.int64)]
+        self._Lleaf = [np.ones(1, dtype=bool)]
 
-        # adaptive refinement
+        # adaptive refinement, level by level
         lev = 0
         while lev < D:
-            to_split = [c for c, rec in levels[lev].items() if rec[1] - rec[0] > self.leaf_size]
-            if not to_split:
+            split = np.flatnonzero(self._Lleaf[lev] & (self._Le[lev] - self._Ls[lev] > self.leaf_size))
+            if split.size == 0:
                 break
-            for c in to_split:
-                self._split(lev, c)
+            self._split_boxes(lev, split)
             lev += 1
 
         # 2:1 balance
@@ -121,86 +136,101 @@ class BalancedTree:
         self._finalize()
 
     # ------------------------------------------------------------------ build
-    def _split(self, lev, coords):
-        rec = self._levels[lev][coords]
-        if not rec[2]:
-            return
-        start, end = rec[0], rec[1]
+    def _lookup(self, lev, coords):
+        """Index within level ``lev`` of the boxes at integer ``coords``, -1 if absent."""
+        n = self._Lk[lev].shape[0]
+        nmax = (1 << lev) - 1
+        valid = np.all((coords >= 0) & (coords <= nmax), axis=1)
+        codes = morton_encode(np.where(valid[:, None], coords, 0), lev)
+        pos = np.searchsorted(self._Lk[lev], codes)
+        posc = np.minimum(pos, max(n - 1, 0))
+        found = valid & (pos < n) & (self._Lk[lev][posc] == codes)
+        return np.where(found, posc, -1)
+
+    def _split_boxes(self, lev, sel):
+        """Split the leaves ``sel`` (indices within level ``lev``): their
+        non-empty children join level ``lev + 1``."""
         D = self._depth
-        ndim = self.ndim
-        if lev + 1 > D:
+        if lev + 1 > D or sel.size == 0:
             return
-        if len(self._levels) <= lev + 1:
-            self._levels.append({})
-        shift = np.uint64(ndim * (D - lev - 1))
-        ck = self._skeys[start:end] >> shift
-        brk = np.flatnonzero(ck[1:] != ck[:-1]) + 1
-        starts = np.concatenate(([0], brk)) + start
-        ends = np.concatenate((brk, [end - start])) + start
-        child_level = self._levels[lev + 1]
-        for s, e in zip(starts.tolist(), ends.tolist()):
-            cc = tuple((self._sq[s] >> (D - lev - 1)).tolist())
-            child_level[cc] = [s, e, True]
-        rec[2] = False
+        starts = self._Ls[lev][sel]
+        ends = self._Le[lev][sel]
+        lens = ends - starts
+        if sel.size == self._Ls[lev].shape[0] and int(lens.sum()) == self.N:
+            idx = np.arange(self.N, dtype=np.int64)
+        else:
+            # concatenated point ranges [start, end) of the boxes
+            before = np.cumsum(lens) - lens
+            idx = np.arange(int(lens.sum()), dtype=np.int64) + np.repeat(starts - before, lens)
+        shift = np.uint64(self.ndim * (D - lev - 1))
+        ck = self._skeys[idx] >> shift
+        brk = np.flatnonzero((ck[1:] != ck[:-1]) | (idx[1:] != idx[:-1] + 1)) + 1
+        first = np.concatenate(([0], brk))
+        cs = idx[first]
+        ce = np.concatenate((idx[brk - 1] + 1, [idx[-1] + 1]))
+        coords = (self._sq[cs] >> (D - lev - 1)).astype(np.int64)
+        codes = ck[first]
+        self._Lleaf[lev][sel] = False
+        if len(self._Lk) <= lev + 1:
+            self._Lc.append(coords)
+            self._Lk.append(codes)
+            self._Ls.append(cs.astype(np.int64))
+            self._Le.append(ce.astype(np.int64))
+            self._Lleaf.append(np.ones(cs.shape[0], dtype=bool))
+            return
+        k = np.concatenate((self._Lk[lev + 1], codes))
+        order = np.argsort(k, kind="stable")
+        self._Lk[lev + 1] = k[order]
+        self._Lc[lev + 1] = np.concatenate((self._Lc[lev + 1], coords))[order]
+        self._Ls[lev + 1] = np.concatenate((self._Ls[lev + 1], cs))[order]
+        self._Le[lev + 1] = np.concatenate((self._Le[lev + 1], ce))[order]
+        self._Lleaf[lev + 1] = np.concatenate((self._Lleaf[lev + 1], np.ones(cs.shape[0], dtype=bool)))[order]
 
     def _balance(self):
+        """Split every leaf at level l-2 that touches a box at level l, until
+        none is left."""
         ndim = self.ndim
+        combos = np.array(list(itertools.product((0, 1), repeat=ndim)), dtype=np.int64)
         changed = True
         while changed:
             changed = False
-            for lev in range(len(self._levels) - 1, 1, -1):
-                coarse = self._levels[lev - 2]
+            for lev in range(len(self._Lk) - 1, 1, -1):
+                C = self._Lc[lev]
+                if C.shape[0] == 0:
+                    continue
                 nmax = (1 << (lev - 2)) - 1
-                marks = set()
-                for c in self._levels[lev].keys():
-                    ranges = []
-                    for b in c:
-                        g0 = max(0, -((4 - b) // 4))  # ceil((b-4)/4)
-                        g1 = min(nmax, (b + 1) // 4)
-                        ranges.append(range(g0, g1 + 1))
-                    for g in itertools.product(*ranges):
-                        rec = coarse.get(g)
-                        if rec is not None and rec[2]:
-                            marks.add(g)
-                for g in marks:
-                    self._split(lev - 2, g)
+                g0 = np.maximum(0, -((4 - C) // 4))  # ceil((b-4)/4)
+                g1 = np.minimum(nmax, (C + 1) // 4)
+                G = (g0[:, None, :] + combos[None, :, :]).reshape(-1, ndim)
+                ok = np.all(G <= np.repeat(g1, combos.shape[0], axis=0), axis=1)
+                codes = np.unique(morton_encode(G[ok], lev - 2))
+                Lk = self._Lk[lev - 2]
+                pos = np.minimum(np.searchsorted(Lk, codes), Lk.shape[0] - 1)
+                pos = pos[Lk[pos] == codes]
+                marks = np.unique(pos[self._Lleaf[lev - 2][pos]])
+                if marks.size:
+                    self._split_boxes(lev - 2, marks)
                     changed = True
 
     def _finalize(self):
         ndim = self.ndim
-        D = self._depth
-        nlev = len(self._levels)
-        while nlev > 0 and not self._levels[nlev - 1]:
+        nlev = len(self._Lk)
+        while nlev > 0 and self._Lk[nlev - 1].shape[0] == 0:
             nlev -= 1
-        self._levels = self._levels[:nlev]
+        for name in ("_Lc", "_Lk", "_Ls", "_Le", "_Lleaf"):
+            setattr(self, name, getattr(self, name)[:nlev])
         self.nlevels = nlev
 
-        coords_all, start_all, end_all, leaf_all, level_all = [], [], [], [], []
         level_sep = np.zeros(nlev + 1, dtype=np.int64)
-        index_of = []
         for lev in range(nlev):
-            items = list(self._levels[lev].items())
-            cs = np.array([k for k, _ in items], dtype=np.int64).reshape(-1, ndim)
-            codes = morton_encode(cs, max(lev, 1))
-            order = np.argsort(codes, kind="stable")
-            cs = cs[order]
-            recs = [items[i][1] for i in order.tolist()]
-            base = level_sep[lev]
-            level_sep[lev + 1] = base + len(recs)
-            index_of.append({tuple(cs[i].tolist()): base + i for i in range(len(recs))})
-            coords_all.append(cs)
-            start_all.append([r[0] for r in recs])
-            end_all.append([r[1] for r in recs])
-            leaf_all.append([r[2] for r in recs])
-            level_all.append(np.full(len(recs), lev, dtype=np.int64))
-
+            level_sep[lev + 1] = level_sep[lev] + self._Lk[lev].shape[0]
         self.level_sep = level_sep
         self.nboxes = int(level_sep[-1])
-        self._box_coords = np.concatenate(coords_all, axis=0)
-        self._box_start = np.concatenate([np.asarray(s, dtype=np.int64) for s in start_all])
-        self._box_end = np.concatenate([np.asarray(s, dtype=np.int64) for s in end_all])
-        self._is_leaf = np.concatenate([np.asarray(s, dtype=bool) for s in leaf_all])
-        self._box_level = np.concatenate(level_all)
+        self._box_coords = np.concatenate(self._Lc, axis=0)
+        self._box_start = np.concatenate(self._Ls)
+        self._box_end = np.concatenate(self._Le)
+        self._is_leaf = np.concatenate(self._Lleaf)
+        self._box_level = np.concatenate([np.full(self._Lk[l].shape[0], l, dtype=np.int64) for l in range(nlev)])
         self._leaves = np.flatnonzero(self._is_leaf).astype(np.int64)
         self.nleaves = int(self._leaves.shape[0])
 
@@ -209,52 +239,48 @@ class BalancedTree:
         children = np.full((nb, nchild), -1, dtype=np.int64)
         parent = np.full(nb, -1, dtype=np.int64)
         for lev in range(1, nlev):
-            pidx = index_of[lev - 1]
-            kids = {}
-            for c, b in index_of[lev].items():
-                p = pidx[tuple(x >> 1 for x in c)]
-                parent[b] = p
-                kids.setdefault(p, []).append(b)
-            for p, bl in kids.items():
-                bl.sort()
-                children[p, : len(bl)] = bl
+            base = level_sep[lev]
+            n = self._Lk[lev].shape[0]
+            pl = self._lookup(lev - 1, self._Lc[lev] >> 1)
+            pg = pl + level_sep[lev - 1]
+            parent[base:base + n] = pg
+            # siblings are contiguous in Morton order
+            firsts = np.concatenate(([0], np.flatnonzero(pg[1:] != pg[:-1]) + 1))
+            slot = np.arange(n) - np.repeat(firsts, np.diff(np.concatenate((firsts, [n]))))
+            children[pg, slot] = base + np.arange(n)
         self._children = children
         self._parent = parent
 
         # colleagues: offsets in {-1,0,1}^d, lexicographic
-        offsets = list(itertools.product((-1, 0, 1), repeat=ndim))
-        ncol = len(offsets)
-        colleagues = np.full((nb, ncol), -1, dtype=np.int64)
+        offsets = np.array(list(itertools.product((-1, 0, 1), repeat=ndim)), dtype=np.int64)
+        colleagues = np.full((nb, offsets.shape[0]), -1, dtype=np.int64)
         coarse = np.full((nb, nchild), -1, dtype=np.int64)
+        pair = np.array(list(itertools.product((0, 1), repeat=ndim)), dtype=np.int64)
         for lev in range(nlev):
-            idx = index_of[lev]
-            nmax = (1 << lev) - 1
-            up = index_of[lev - 1] if lev > 0 else None
-            nmax_up = (1 << (lev - 1)) - 1 if lev > 0 else -1
-            for c, b in idx.items():
-                for k, off in enumerate(offsets):
-                    n = tuple(ci + oi for ci, oi in zip(c, off))
-                    if min(n) < 0 or max(n) > nmax:
-                        continue
-                    nbx = idx.get(n)
-                    if nbx is not None:
-                        colleagues[b, k] = nbx
-                if up is None:
-                    continue
-                ranges = []
-                for x in c:
-                    g0 = max(0, -((2 - x) // 2))  # ceil((x-2)/2)
-                    g1 = min(nmax_up, (x + 1) // 2)
-                    ranges.append(range(g0, g1 + 1))
-                acc = 0
-                par = tuple(x >> 1 for x in c)
-                for g in itertools.product(*ranges):
-                    if g == par:
-                        continue
-                    nbx = up.get(g)
-                    if nbx is not None and self._is_leaf[nbx]:
-                        coarse[b, acc] = nbx
-                        acc += 1
+            base = level_sep[lev]
+            C = self._Lc[lev]
+            n = C.shape[0]
+            for k in range(offsets.shape[0]):
+                pos = self._lookup(lev, C + offsets[k][None, :])
+                colleagues[base:base + n, k] = np.where(pos >= 0, pos + base, -1)
+            if lev == 0:
+                continue
+            # coarse neighbours: leaves one level up touching the box, parent excluded
+            nmax_up = (1 << (lev - 1)) - 1
+            g0 = np.maximum(0, -((2 - C) // 2))  # ceil((x-2)/2)
+            g1 = np.minimum(nmax_up, (C + 1) // 2)
+            par = C >> 1
+            found = np.full((n, pair.shape[0]), -1, dtype=np.int64)
+            for t in range(pair.shape[0]):
+                G = g0 + pair[t][None, :]
+                ok = np.all(G <= g1, axis=1) & ~np.all(G == par, axis=1)
+                pos = self._lookup(lev - 1, np.where(ok[:, None], G, -1))
+                gpos = pos + level_sep[lev - 1]
+                keep = (pos >= 0) & self._is_leaf[np.where(pos >= 0, gpos, 0)]
+                found[:, t] = np.where(keep, gpos, -1)
+            # compact each row, keeping the enumeration order
+            order = np.argsort(found < 0, axis=1, kind="stable")
+            coarse[base:base + n] = np.take_along_axis(found, order, axis=1)
         self._colleagues = colleagues
         self._coarse = coarse
 
@@ -405,6 +431,7 @@ POINT_GEOMETRIES = (
     "sphere_surface",
     "annulus",
     "curvy_annulus",
+    "gaussian_clusters",
 )
 
 
@@ -439,4 +466,11 @@ def get_point_dist(N, name, rng=None):
         th = 2 * np.pi * rand(N)
         r = rho * (1 + 0.25 * np.cos(6 * th)) if name == "curvy_annulus" else rho
         return np.stack((r * np.cos(th), r * np.sin(th)), axis=1)
+    if name == "gaussian_clusters":
+        # 32 isotropic Gaussian clusters, centres uniform in the unit cube,
+        # standard deviations log-uniform in [1e-3, 5e-2]
+        centres = rand(32, 3)
+        sigma = np.exp(np.log(1e-3) + (np.log(5e-2) - np.log(1e-3)) * rand(32))
+        which = np.minimum((rand(N) * 32).astype(np.int64), 31)
+        return centres[which] + sigma[which, None] * randn(N, 3)
     raise ValueError(f"Unknown geometry {name!r}. Available: {', '.join(POINT_GEOMETRIES)}")
