@@ -14,6 +14,7 @@
  *   skf_skel_boxes      util.skel_box_helper over a level skelfmm/util.py:381-437,
  *                       driven by RecursiveSkeletonization.skel_tree
  *                       skelfmm/recursive_skel.py:412-492
+ *   skf_proxy_rows      proxy surface size, skelfmm/util.py:72-78 + 87-124
  */
 #ifndef SKF_H
 #define SKF_H
@@ -88,6 +89,8 @@ typedef struct {
   const int64_t* list_off;     /* [nboxes+1] per-target interaction lists */
   const int32_t* list_src;     /* [L] source box */
   const int8_t* list_kind;     /* [L] SKF_KIND_* */
+  int32_t t_on_device;         /* 1: t_data is a DEVICE pointer (copied device to
+                                  device), 0: host pointer like the rest */
 } skf_plan_desc;
 
 typedef struct {
@@ -177,6 +180,63 @@ int skf_skel_boxes_noalloc(int32_t op, double kappa, int32_t nbox, const int64_t
                            const double* geom, const double* centers, double box_length, int32_t nproxy,
                            double tol, int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out,
                            void* stream);
+
+/* Device segmented copy (build bookkeeping: compacting T blocks written at
+   capacity offsets): dst[dst_off[s] + i] = src[src_off[s] + i], i < len[s],
+   offsets and lengths in elements of `elem_bytes` (8 or 16).  All DEVICE. */
+int skf_copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_off, const int64_t* len,
+                      const void* src, void* dst, int32_t elem_bytes, void* stream);
+
+/* Number of rows of the stacked proxy matrix the build uses for `nproxy`
+   requested proxy points (cube/sphere surface size, doubled for the
+   geometry operators). */
+int skf_proxy_rows(int32_t op, int32_t nproxy, int32_t* rows_out);
+
+/*
+ * Randomized proxy IDs — the learned-rank build's fast path; no counterpart
+ * in the reference, whose IDs are skf_skel_boxes.  Same arguments and outputs
+ * as skf_skel_boxes (tol < 1), plus, all DEVICE unless noted:
+ *   kpred[nbox]  predicted rank of box b (<= 0: full pivoted-QR ID).  The box
+ *                factors sketches Y = S K of its proxy matrix K, S a sparse
+ *                sign matrix with `rho` +-1 entries per row at hashed proxy
+ *                rows (from `seed`), first with kpred[b] + oversample rows,
+ *                doubling while the rank found on Y with |R_kk| <= sketch_tol
+ *                |R_00| comes within oversample/2 of the sketch size (or
+ *                until the sketch would exceed half of K's rows).  The ID of
+ *                the first unsaturated sketch is kept when its relative
+ *                Frobenius residual on `nchk` hashed rows of K is <=
+ *                resid_tol; otherwise the box falls back to the full
+ *                pivoted-QR ID of K with the tol rule.
+ *   resid[nbox]  (out, may be NULL) that residual; -1 not tried, -2 every
+ *                sketch saturated.
+ *   status[nbox] (out, may be NULL) 0 full QR; else 10 * (sketches tried) +
+ *                1 (randomized ID kept) or 2 (rejected, full QR used).
+ */
+int skf_skel_boxes_randomized(int32_t op, double kappa, int32_t nbox, const int64_t* off, const double* x,
+                              const double* geom, const double* centers, double box_length, int32_t nproxy,
+                              double tol, const int32_t* kpred, int32_t oversample, int32_t rho, uint64_t seed,
+                              int32_t nchk, double sketch_tol, double resid_tol, double* resid, int8_t* status,
+                              int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out, void* stream);
+
+/*
+ * Rank predictor of the learned-rank build (no counterpart in the
+ * reference): a 3-layer perceptron of width 128 with BF16 weights and
+ * activations, trained on log2(rank + 1) of pivoted-QR builds.  Parameters
+ * are one vector (FP32 master `theta`, BF16 mirror `theta16`) laid out as
+ * W1[128 x nin] b1[128] W2[128 x 128] b2[128] w3[128] b3[1]; inputs are
+ * BF16 [n x nin], nin <= 32.  All pointers DEVICE.
+ */
+int64_t skf_mlp_num_params(int32_t nin);                 /* -1 if nin is out of range */
+int64_t skf_mlp_scratch_floats(int32_t nin, int64_t n);  /* scratch of skf_mlp_train_step */
+int skf_mlp_bf16(const float* src, void* dst, int64_t n, void* stream);  /* FP32 -> BF16 */
+int skf_mlp_predict(int32_t nin, const void* theta16, const void* x16, int64_t n, float* y, void* stream);
+/* One full-batch step: grad = d/dtheta mean((y - target)^2) (deterministic
+   order); with apply != 0 also an Adam step (bias-corrected, `step` >= 1) on
+   theta, adam_m, adam_v and the BF16 mirror.  loss (may be NULL) = the
+   batch's mean squared error before the step. */
+int skf_mlp_train_step(int32_t nin, float* theta, void* theta16, const void* x16, const float* target, int64_t n,
+                       float* scratch, float* grad, float* adam_m, float* adam_v, int32_t step, float lr,
+                       float beta1, float beta2, float eps, int32_t apply, float* loss, void* stream);
 
 const char* skf_status_string(int32_t status);
 int skf_version(void);

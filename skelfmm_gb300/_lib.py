@@ -35,6 +35,7 @@ _p = ctypes.c_void_p
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
 _f64 = ctypes.c_double
+_f32 = ctypes.c_float
 
 
 class PlanDesc(ctypes.Structure):
@@ -45,7 +46,7 @@ class PlanDesc(ctypes.Structure):
         ("entry_xyz", _p), ("entry_geom", _p), ("entry_pslot", _p),
         ("nperm", _i64), ("perm_entry", _p), ("perm_point", _p),
         ("t_off", _p), ("t_data", _p), ("t_len", _i64),
-        ("list_off", _p), ("list_src", _p), ("list_kind", _p),
+        ("list_off", _p), ("list_src", _p), ("list_kind", _p), ("t_on_device", _i32),
     ]
 
 
@@ -71,6 +72,16 @@ SIGNATURES = {
     "skf_kernel_apply": (_i32, [_i32, _f64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _p, _p, _p, _p, _i32, _p]),
     "skf_skel_boxes": (_i32, [_i32, _f64, _i32, _p, _p, _p, _p, _f64, _i32, _f64, _p, _p, _p, _p, _p]),
     "skf_skel_boxes_noalloc": (_i32, [_i32, _f64, _i32, _p, _p, _p, _p, _f64, _i32, _f64, _p, _p, _p, _p, _p]),
+    "skf_proxy_rows": (_i32, [_i32, _i32, ctypes.POINTER(_i32)]),
+    "skf_skel_boxes_randomized": (_i32, [_i32, _f64, _i32, _p, _p, _p, _p, _f64, _i32, _f64, _p, _i32, _i32,
+                                         ctypes.c_uint64, _i32, _f64, _f64, _p, _p, _p, _p, _p, _p, _p]),
+    "skf_copy_segments": (_i32, [_i64, _p, _p, _p, _p, _p, _i32, _p]),
+    "skf_mlp_num_params": (_i64, [_i32]),
+    "skf_mlp_scratch_floats": (_i64, [_i32, _i64]),
+    "skf_mlp_bf16": (_i32, [_p, _p, _i64, _p]),
+    "skf_mlp_predict": (_i32, [_i32, _p, _p, _i64, _p, _p]),
+    "skf_mlp_train_step": (_i32, [_i32, _p, _p, _p, _p, _i64, _p, _p, _p, _p, _i32, _f32, _f32, _f32, _f32,
+                                  _i32, _p, _p]),
 }
 
 _lib = None

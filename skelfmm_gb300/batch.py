@@ -57,7 +57,7 @@ def concat_ragged(rbs):
         eoff += rb.nentries
         boff += nb
         poff += rb.npoints
-        toff += rb.t_data.shape[0]
+        toff += int(rb.t_data.shape[0])
         loff += int(rb.list_off[-1])
         starts.append(poff)
     out = RaggedBuild(
@@ -65,9 +65,14 @@ def concat_ragged(rbs):
         box_level=np.concatenate(box_level), box_off=np.concatenate(box_off), box_rank=np.concatenate(box_rank),
         entry_xyz=np.concatenate(xyz), entry_geom=np.concatenate(geom) if geom else None,
         entry_pslot=np.concatenate(pslot), perm_entry=np.concatenate(pe), perm_point=np.concatenate(pp),
-        t_off=np.concatenate(t_off), t_data=np.concatenate(t_data), list_off=np.concatenate(list_off),
+        t_off=np.concatenate(t_off), t_data=None, list_off=np.concatenate(list_off),
         list_src=np.concatenate(list_src).astype(np.int32), list_kind=np.concatenate(list_kind),
     )
+    if not any(isinstance(t, torch.Tensor) for t in t_data):
+        out.t_data = np.concatenate(t_data)
+    else:
+        dev = next(t.device for t in t_data if isinstance(t, torch.Tensor))
+        out.t_data = torch.cat([t if isinstance(t, torch.Tensor) else torch.from_numpy(t).to(dev) for t in t_data])
     return out, np.asarray(starts, dtype=np.int64)
 
 

@@ -263,7 +263,7 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
           c.u = p->u;
           c.uh = p->uh;
           if (p->worksym.n > 0) k_translate_sym<OP><<<p->worksym.n, 128, 0, st>>>(c);
-          k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3((p->max_bs + 255) / 256, p->nboxes), 256, 0, st>>>(
+          k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
               p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
           return;
         }
@@ -305,6 +305,45 @@ static int grid_for(int64_t n, int threads) {
   if (g < 1) g = 1;
   if (g > 152 * 32) g = 152 * 32;
   return (int)g;
+}
+
+__global__ void k_f64_to_f32(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+// dst[dst_off[s] + i] = src[src_off[s] + i] for i < len[s]; elements of
+// 8 (W = 1) or 16 (W = 2) bytes.  One block per segment (grid-strided).
+template <int W>
+__global__ void k_copy_segments(int64_t nseg, const int64_t* __restrict__ src_off,
+                                const int64_t* __restrict__ dst_off, const int64_t* __restrict__ len,
+                                const double* __restrict__ src, double* __restrict__ dst) {
+  for (int64_t sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+    const int64_t so = src_off[sgi] * W, d0 = dst_off[sgi] * W, n = len[sgi] * W;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) dst[d0 + i] = src[so + i];
+  }
+}
+
+int copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_off, const int64_t* len,
+                  const void* src, void* dst, int elem_bytes, cudaStream_t st) {
+  if (nseg <= 0) return SKF_OK;
+  const int g = (int)std::min<int64_t>(nseg, 152 * 16);
+  if (elem_bytes == 8)
+    k_copy_segments<1><<<g, 256, 0, st>>>(nseg, src_off, dst_off, len, static_cast<const double*>(src),
+                                          static_cast<double*>(dst));
+  else
+    k_copy_segments<2><<<g, 256, 0, st>>>(nseg, src_off, dst_off, len, static_cast<const double*>(src),
+                                          static_cast<double*>(dst));
+  SKF_CUDA_TRY(cudaGetLastError());
+  return SKF_OK;
+}
+
+int convert_f64_f32(const double* src, float* dst, int64_t n, cudaStream_t st) {
+  if (n <= 0) return SKF_OK;
+  k_f64_to_f32<<<grid_for(n, 256), 256, 0, st>>>(src, dst, n);
+  SKF_CUDA_TRY(cudaGetLastError());
+  SKF_CUDA_TRY(cudaStreamSynchronize(st));
+  return SKF_OK;
 }
 
 // precision: SKF_PREC_FP64, SKF_PREC_MIXED (FP32 kernel evaluation, FP64 T),
@@ -382,8 +421,8 @@ __global__ void k_block_apply(int npairs, int mmax, int nmax, const int32_t* __r
   constexpr bool C = OpTraits<OP>::kComplex;
   constexpr int D = OpTraits<OP>::kDim;
   constexpr int G = OpTraits<OP>::kGeom;
-  const int pr = blockIdx.y;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int pr = blockIdx.x;
+  const int i = blockIdx.y * blockDim.x + threadIdx.x;
   if (pr >= npairs || i >= m[pr]) return;
   const int nn = n[pr];
   const bool self = self_flag != nullptr && self_flag[pr] != 0;
@@ -443,7 +482,7 @@ template <int OP>
 static void launch_block(int npairs, int mmax, int nmax, const int32_t* m, const int32_t* n, const double* xt,
                          const double* xs, const double* gt, const double* gs, const double* q, const int8_t* sf,
                          double* out, double kappa, bool mixed, cudaStream_t st) {
-  dim3 grid((mmax + 127) / 128, npairs);
+  dim3 grid(npairs, (mmax + 127) / 128);  // pairs on x (2^31 - 1), row tiles on y
   if (mixed) k_block_apply<OP, true><<<grid, 128, 0, st>>>(npairs, mmax, nmax, m, n, xt, xs, gt, gs, q, sf, out, kappa);
   else k_block_apply<OP, false><<<grid, 128, 0, st>>>(npairs, mmax, nmax, m, n, xt, xs, gt, gs, q, sf, out, kappa);
 }

@@ -105,6 +105,25 @@ struct SkelArgs {
   const int64_t* t_off_out;
   double* t_out;
   int first_box;
+  // randomized mode: box b with kpred[b] > 0 first factors sketches
+  // Y = S K of its proxy matrix (S a sparse sign matrix with `rho` nonzeros
+  // per row drawn from `seed`), starting with kpred[b] + oversample rows and
+  // doubling while the rank found on Y (|R_kk| <= sketch_tol |R_00|) comes
+  // within `oversample / 2` of the sketch size; the ID of the first
+  // unsaturated sketch is checked on nchk hashed rows of K and kept when its
+  // relative Frobenius residual is <= resid_tol, else the box runs the full
+  // pivoted-QR ID of K.
+  const int32_t* kpred;
+  int oversample;
+  int rho;
+  uint64_t seed;
+  int nchk;
+  double sketch_tol;
+  double resid_tol;
+  double* resid;    // [nbox] residual of the randomized ID (-1: not tried)
+  int8_t* status;   // [nbox] 0 full QR; else 10 * sketch rounds + (1 kept, 2 rejected)
+  int64_t ycap;     // doubles of dynamic shared memory for the sketch (0: none)
+  const int32_t* order;  // block -> box of the batch, longest first (NULL: identity)
 };
 
 constexpr int kSkelThreads = 256;
@@ -120,90 +139,94 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return s;
 }
 
+// Entry (row i, box point x) of the stacked proxy matrix: rows [0, np) are
+// K(x, p_i) (target = box point), rows [np, 2 np) of the geometry operators
+// K(p_i, x) (target = proxy).  Sphere proxies carry radial normals.
 template <int OP>
-__global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
-  constexpr bool C = OpTraits<OP>::kComplex;
+__device__ __forceinline__ void proxy_entry(const SkelArgs& a, const double (&c)[3], int i, const double* xj,
+                                            const double* gj, double& kr, double& ki) {
   constexpr int D = OpTraits<OP>::kDim;
   constexpr int G = OpTraits<OP>::kGeom;
-  constexpr int W = C ? 2 : 1;  // scalars per matrix entry
-  extern __shared__ double sm[];
-  const int b = a.first_box + blockIdx.x;
-  const int64_t off = a.off[b];
-  const int n = (int)(a.off[b + 1] - off);
-  const int m = a.mrows;
-  // smem: vn1[n], vn2[n], v[m*W], red[64], misc
-  double* vn1 = sm;
-  double* vn2 = vn1 + n;
-  double* vv = vn2 + n;
-  double* red = vv + (size_t)m * W;
-  int* piv = reinterpret_cast<int*>(red + 64);
+  const int pi = (i < a.np) ? i : i - a.np;
+  double p[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) p[d] = c[d] + a.plen * a.tmpl[pi * D + d];
+  double gx = 0, gy = 0, gz = 0;
+  double pn[3] = {0, 0, 0};
+  if (G != 0) {
+    double nn = 0;
+    for (int d = 0; d < D; ++d) {
+      pn[d] = p[d] - c[d];
+      nn += pn[d] * pn[d];
+    }
+    nn = sqrt(nn);
+    for (int d = 0; d < D; ++d) pn[d] /= nn;
+  }
+  if (G == 0 || i >= a.np) {
+    // K(x_j, p_i): target = box point, source = proxy
+    if (G == 1) { gx = pn[0]; gy = pn[1]; gz = pn[2]; }
+    if (G == 2) { gx = gj[0]; gy = gj[1]; gz = gj[2]; }
+    eval_f64<OP>(xj[0] - p[0], xj[1] - p[1], D == 3 ? xj[2] - p[2] : 0.0, gx, gy, gz, a.kappa, kr, ki);
+  } else {
+    // K(p_i, x_j): target = proxy, source = box point
+    if (G == 1) { gx = gj[0]; gy = gj[1]; gz = gj[2]; }
+    if (G == 2) { gx = pn[0]; gy = pn[1]; gz = pn[2]; }
+    eval_f64<OP>(p[0] - xj[0], p[1] - xj[1], D == 3 ? p[2] - xj[2] : 0.0, gx, gy, gz, a.kappa, kr, ki);
+  }
+}
+
+// 64-bit mixing function (splitmix64 finaliser) for the sketch's indices.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+struct QrScratch {
+  double* vn1;  // [n] squared partial column norms
+  double* vn2;  // [n] squared norms at the last recomputation
+  double* vv;   // [m * W] Householder vector
+  double* red;  // [64] reduction scratch
+  int* piv;     // [n] column permutation
+};
+
+// Column-pivoted Householder QR of the m x n column-major matrix A (leading
+// dimension m), stopped at rank kfix (> 0) or at |R_kk| <= tol |R_00|.
+// Businger-Golub pivoting (first index of the largest partial norm), partial
+// norms downdated as in LAPACK's xLAQP2 (LAWN 176), kept squared: the
+// downdate vn1^2 - |r_kj|^2 and LAPACK's recompute test
+// (1 - (|r_kj| / vn1)^2) (vn1 / vn2)^2 <= sqrt(eps), i.e.
+// vn1^2 - |r_kj|^2 <= sqrt(eps) vn2^2, need no division or square root.
+// On return A holds R in its upper triangle (rows < rank) and the updated
+// trailing block; piv the column order.  Returns the rank.
+template <int OP>
+__device__ int pivoted_qr(double* A, int m, int n, double tol, int kfix, const QrScratch& q) {
+  constexpr bool C = OpTraits<OP>::kComplex;
+  constexpr int W = C ? 2 : 1;
   __shared__ int s_k;
   __shared__ double s_scal[4];
-
-  double* A = a.ws + a.ws_off[blockIdx.x];
+  double* vn1 = q.vn1;
+  double* vn2 = q.vn2;
+  double* vv = q.vv;
+  double* red = q.red;
+  int* piv = q.piv;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double c[3] = {0, 0, 0};
-  for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
-
-  // ---- 1. proxy matrix, column j = box point j
-  for (int64_t idx = threadIdx.x; idx < (int64_t)m * n; idx += blockDim.x) {
-    const int j = (int)(idx / m), i = (int)(idx % m);
-    const double* xj = a.x + (off + j) * D;
-    const int pi = (i < a.np) ? i : i - a.np;
-    double p[3] = {0, 0, 0};
-    for (int d = 0; d < D; ++d) p[d] = c[d] + a.plen * a.tmpl[pi * D + d];
-    double gx = 0, gy = 0, gz = 0;
-    double kr, ki;
-    // proxy normals (sphere proxies) are radial
-    double pn[3] = {0, 0, 0};
-    if (G != 0) {
-      double nn = 0;
-      for (int d = 0; d < D; ++d) {
-        pn[d] = p[d] - c[d];
-        nn += pn[d] * pn[d];
-      }
-      nn = sqrt(nn);
-      for (int d = 0; d < D; ++d) pn[d] /= nn;
-    }
-    if (G == 0 || i >= a.np) {
-      // K(x_j, p_i): target = box point, source = proxy
-      if (G == 1) { gx = pn[0]; gy = pn[1]; gz = pn[2]; }
-      if (G == 2) {
-        const double* g = a.geom + (off + j) * 3;
-        gx = g[0]; gy = g[1]; gz = g[2];
-      }
-      eval_f64<OP>(xj[0] - p[0], xj[1] - p[1], D == 3 ? xj[2] - p[2] : 0.0, gx, gy, gz, a.kappa, kr, ki);
-    } else {
-      // K(p_i, x_j): target = proxy, source = box point
-      if (G == 1) {
-        const double* g = a.geom + (off + j) * 3;
-        gx = g[0]; gy = g[1]; gz = g[2];
-      }
-      if (G == 2) { gx = pn[0]; gy = pn[1]; gz = pn[2]; }
-      eval_f64<OP>(p[0] - xj[0], p[1] - xj[1], D == 3 ? p[2] - xj[2] : 0.0, gx, gy, gz, a.kappa, kr, ki);
-    }
-    A[((int64_t)j * m + i) * W] = kr;
-    if (C) A[((int64_t)j * m + i) * W + 1] = ki;
-  }
-  __syncthreads();
-  // column norms
   for (int j = warp; j < n; j += nw) {
     double s = 0;
     const double* col = A + (int64_t)j * m * W;
     for (int i = lane; i < m * W; i += 32) s += col[i] * col[i];
     s = warp_sum_d(s);
     if (lane == 0) {
-      vn1[j] = sqrt(s);
-      vn2[j] = vn1[j];
+      vn1[j] = s;
+      vn2[j] = s;
     }
   }
   for (int j = threadIdx.x; j < n; j += blockDim.x) piv[j] = j;
   __syncthreads();
 
-  // ---- 2. column-pivoted Householder QR
   const int kmax = min(m, n);
-  const bool fixed = a.tol >= 1.0;
-  const int rank_fixed = fixed ? min((int)a.tol, kmax) : kmax;
+  const bool fixed = kfix > 0;
+  const int rank_fixed = fixed ? min(kfix, kmax) : kmax;
   double r00 = 0.0;
   int rank = 0;
   const double tol3z = sqrt(2.220446049250313e-16);
@@ -302,7 +325,7 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
     const double scr = red[60], sci = red[61];
     if (k == 0) r00 = fabs(beta);
     const double rkk = fabs(beta);
-    const bool stop = fixed ? (k >= rank_fixed) : (!(rkk > a.tol * r00) || r00 == 0.0);
+    const bool stop = fixed ? (k >= rank_fixed) : (!(rkk > tol * r00) || r00 == 0.0);
     if (stop) {
       rank = k;
       break;
@@ -361,35 +384,46 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
         akj2 = ar * ar + ai * ai;
       }
       const double v1 = vn1[j];
-      double temp = 0.0;
-      bool recompute = false;
-      if (v1 != 0.0) {
-        temp = 1.0 - akj2 / (v1 * v1);
-        temp = temp < 0 ? 0 : temp;
-        const double ratio = v1 / vn2[j];
-        recompute = temp * ratio * ratio <= tol3z;
-      }
+      const double rem = v1 - akj2;
+      const bool recompute = v1 != 0.0 && rem <= tol3z * vn2[j];
       if (recompute) {
         part = warp_sum_d(part);
         if (lane == 0) {
-          vn1[j] = sqrt(part);
-          vn2[j] = vn1[j];
+          vn1[j] = part;
+          vn2[j] = part;
         }
       } else if (lane == 0 && v1 != 0.0) {
-        vn1[j] = v1 * sqrt(temp);
+        vn1[j] = rem;
       }
       __syncwarp();
     }
     __syncthreads();
   }
   __syncthreads();
-  // ---- 3. outputs: rank, permutation, T = R11^{-1} R12 (row-major rank x (n-rank))
-  if (threadIdx.x == 0) a.rank[b] = rank;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) a.perm[off + j] = piv[j];
+  return rank;
+}
+
+// T = R11^{-1} R12 (row-major rank x (n - rank)) from the R that pivoted_qr
+// left in A: column back substitution, one warp per right-hand side.
+template <int OP>
+__device__ void write_T(double* A, int m, int n, int rank, double* T, double* rinv) {
+  constexpr bool C = OpTraits<OP>::kComplex;
+  constexpr int W = C ? 2 : 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int nr = n - rank;
-  double* T = a.t_out + a.t_off_out[b] * W;
+  // reciprocals of the diagonal of R11 (rinv: [rank * W] shared scratch)
+  for (int i = threadIdx.x; i < rank; i += blockDim.x) {
+    const double rr = A[((int64_t)i * m + i) * W], ri = C ? A[((int64_t)i * m + i) * W + 1] : 0.0;
+    if (C) {
+      const double dd = rr * rr + ri * ri;
+      rinv[2 * i] = rr / dd;
+      rinv[2 * i + 1] = -ri / dd;
+    } else {
+      rinv[i] = 1.0 / rr;
+    }
+  }
+  __syncthreads();
   if (rank > 0 && nr > 0) {
-    // column-oriented back substitution, one warp per right-hand side
     for (int cidx = warp; cidx < nr; cidx += nw) {
       double* bcol = A + (int64_t)(rank + cidx) * m * W;  // R12(:, c), overwritten by t
       for (int i = rank - 1; i >= 0; --i) {
@@ -397,13 +431,12 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
         double tr, ti = 0;
         {
           const double br = bcol[i * W], bi = C ? bcol[i * W + 1] : 0.0;
-          const double rr = ci[i * W], ri = C ? ci[i * W + 1] : 0.0;
           if (C) {
-            const double dd = rr * rr + ri * ri;
-            tr = (br * rr + bi * ri) / dd;
-            ti = (bi * rr - br * ri) / dd;
+            const double qr = rinv[2 * i], qi = rinv[2 * i + 1];
+            tr = br * qr - bi * qi;
+            ti = br * qi + bi * qr;
           } else {
-            tr = br / rr;
+            tr = br * rinv[i];
           }
         }
         __syncwarp();
@@ -424,12 +457,136 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
       }
     }
   }
+  __syncthreads();
 }
 
 template <int OP>
-static int launch_skel(SkelArgs a, int nbox, int maxn, cudaStream_t st) {
+__global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
+  constexpr bool C = OpTraits<OP>::kComplex;
+  constexpr int D = OpTraits<OP>::kDim;
+  constexpr int W = C ? 2 : 1;  // scalars per matrix entry
+  extern __shared__ double sm[];
+  const int lb = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;  // box within the batch
+  const int b = a.first_box + lb;
+  const int64_t off = a.off[b];
+  const int n = (int)(a.off[b + 1] - off);
+  const int m = a.mrows;
+  const int kp = a.kpred ? a.kpred[b] : 0;
+  // randomized ID while the sketch is well below the proxy matrix
+  int s = kp > 0 ? kp + a.oversample : 0;
+  const bool sketch = kp > 0 && 2 * s <= m && kp < n;
+  // smem: vn1[n], vn2[n], v[m * W], red[64], sketch[ycap], piv[n]
+  QrScratch q;
+  q.vn1 = sm;
+  q.vn2 = q.vn1 + n;
+  q.vv = q.vn2 + n;
+  q.red = q.vv + (size_t)m * W;
+  double* sY = q.red + 64;
+  q.piv = reinterpret_cast<int*>(sY + a.ycap);
+
+  double* A = a.ws + a.ws_off[lb];
+  double c[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
+
+  // ---- 1. proxy matrix, column j = box point j
+  for (int64_t idx = threadIdx.x; idx < (int64_t)m * n; idx += blockDim.x) {
+    const int j = (int)(idx / m), i = (int)(idx % m);
+    double kr, ki;
+    proxy_entry<OP>(a, c, i, a.x + (off + j) * D, a.geom ? a.geom + (off + j) * 3 : nullptr, kr, ki);
+    A[((int64_t)j * m + i) * W] = kr;
+    if (C) A[((int64_t)j * m + i) * W + 1] = ki;
+  }
+  __syncthreads();
+
+  double* T = a.t_out + a.t_off_out[b] * W;
+  int rank = 0;
+  bool done = false;
+  if (sketch) {
+    // ---- 2a. sketches Y = S K (s x n, after K in the workspace): row t of
+    // S has rho entries +-1 at hashed proxy rows; doubled while saturated
+    double* gY = A + (int64_t)m * n * W;
+    double* Y = gY;
+    const int guard = max(2, a.oversample / 2);
+    bool ok = false;
+    int rounds = 0;
+    for (int round = 0; 2 * s <= m; ++round, s *= 2) {
+      rounds = round + 1;
+      // the sketch lives in shared memory when it fits (latency-bound QR)
+      Y = ((int64_t)s * n * W <= a.ycap) ? sY : gY;
+      const uint64_t key = mix64(a.seed ^ ((uint64_t)b << 20) ^ ((uint64_t)round << 52));
+      for (int64_t idx = threadIdx.x; idx < (int64_t)s * n; idx += blockDim.x) {
+        const int j = (int)(idx / s), t = (int)(idx % s);
+        double yr = 0, yi = 0;
+        const double* col = A + (int64_t)j * m * W;
+        for (int u = 0; u < a.rho; ++u) {
+          const uint64_t h = mix64(key + (uint64_t)t * 0x100000001B3ull + (uint64_t)u);
+          const int i = (int)((h >> 1) % (uint64_t)m);
+          const double sg = (h & 1) ? -1.0 : 1.0;
+          yr += sg * col[(int64_t)i * W];
+          if (C) yi += sg * col[(int64_t)i * W + 1];
+        }
+        Y[((int64_t)j * s + t) * W] = yr;
+        if (C) Y[((int64_t)j * s + t) * W + 1] = yi;
+      }
+      __syncthreads();
+      rank = pivoted_qr<OP>(Y, s, n, a.sketch_tol, 0, q);
+      if (rank < n && rank > s - guard) continue;  // saturated: the sketch hides rank
+      ok = true;
+      break;
+    }
+    if (ok) {
+      write_T<OP>(Y, s, n, rank, T, q.vn1);
+      // ---- 2b. residual on nchk hashed rows of K (K is still intact)
+      const uint64_t key = mix64(a.seed ^ ((uint64_t)b << 20));
+      const int nr = n - rank;
+      double e2 = 0.0, z2 = 0.0;
+      for (int qi = 0; qi < a.nchk; ++qi) {
+        const int row = (int)((mix64(key ^ (0xC0FFEEull + (uint64_t)qi)) >> 1) % (uint64_t)m);
+        for (int jr = threadIdx.x; jr < n; jr += blockDim.x) {
+          const int pj = q.piv[jr];
+          const double zr = A[((int64_t)pj * m + row) * W], zi = C ? A[((int64_t)pj * m + row) * W + 1] : 0.0;
+          z2 += zr * zr + zi * zi;
+          if (jr < rank) continue;
+          double er = zr, ei = zi;
+          for (int i = 0; i < rank; ++i) {
+            const int pi = q.piv[i];
+            const double sr = A[((int64_t)pi * m + row) * W], si = C ? A[((int64_t)pi * m + row) * W + 1] : 0.0;
+            const double tr = T[((int64_t)i * nr + (jr - rank)) * W];
+            const double ti = C ? T[((int64_t)i * nr + (jr - rank)) * W + 1] : 0.0;
+            er -= sr * tr - si * ti;
+            if (C) ei -= sr * ti + si * tr;
+          }
+          e2 += er * er + ei * ei;
+        }
+      }
+      e2 = block_sum(e2, q.red);
+      z2 = block_sum(z2, q.red);
+      const double res = z2 > 0.0 ? sqrt(e2 / z2) : 0.0;
+      done = res <= a.resid_tol;
+      if (threadIdx.x == 0 && a.resid) a.resid[b] = res;
+    } else if (threadIdx.x == 0 && a.resid) {
+      a.resid[b] = -2.0;  // every sketch saturated
+    }
+    if (threadIdx.x == 0 && a.status) a.status[b] = (int8_t)(10 * rounds + (done ? 1 : 2));
+    __syncthreads();
+  } else if (threadIdx.x == 0) {
+    if (a.resid) a.resid[b] = -1.0;
+    if (a.status) a.status[b] = 0;
+  }
+  if (!done) {
+    // ---- 3. full column-pivoted QR ID of K
+    rank = pivoted_qr<OP>(A, m, n, a.tol >= 1.0 ? 0.0 : a.tol, a.tol >= 1.0 ? (int)a.tol : 0, q);
+    write_T<OP>(A, m, n, rank, T, q.vn1);
+  }
+  if (threadIdx.x == 0) a.rank[b] = rank;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) a.perm[off + j] = q.piv[j];
+}
+
+template <int OP>
+static int launch_skel(SkelArgs a, int nbox, int maxn, int maxm, cudaStream_t st) {
   constexpr int W = OpTraits<OP>::kComplex ? 2 : 1;
-  const size_t smem = sizeof(double) * ((size_t)2 * maxn + (size_t)a.mrows * W + 64) + sizeof(int) * (size_t)maxn;
+  const size_t smem =
+      sizeof(double) * ((size_t)2 * maxn + (size_t)maxm * W + 64 + (size_t)a.ycap) + sizeof(int) * (size_t)maxn;
   if (smem > 200 * 1024) return SKF_ERR_UNSUPPORTED;
   if (smem > 48 * 1024) SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_skel_box<OP><<<nbox, kSkelThreads, smem, st>>>(a);
@@ -437,9 +594,29 @@ static int launch_skel(SkelArgs a, int nbox, int maxn, cudaStream_t st) {
   return SKF_OK;
 }
 
-int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
-               const double* centers, double box_length, int nproxy, double tol, int32_t* rank, int32_t* perm,
-               const int64_t* t_off_out, void* t_out, cudaStream_t st) {
+int proxy_rows(int op, int nproxy) {
+  const int ndim = (op == SKF_LAPLACE_2D || op == SKF_HELMHOLTZ_2D) ? 2 : 3;
+  const bool geom_op = op >= SKF_LAPLACE_DOUBLE_LAYER_3D;
+  const int np = (int)(proxy_template(ndim, geom_op, nproxy).size() / ndim);
+  return geom_op ? 2 * np : np;
+}
+
+struct RandomizedArgs {
+  const int32_t* kpred = nullptr;  // DEVICE [nbox], <= 0: full QR
+  int oversample = 10;
+  int rho = 24;
+  uint64_t seed = 0;
+  int nchk = 16;
+  double sketch_tol = 0.0;
+  double resid_tol = 0.0;
+  double* resid = nullptr;
+  int8_t* status = nullptr;
+};
+
+static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
+                           const double* centers, double box_length, int nproxy, double tol,
+                           const RandomizedArgs& ra, int32_t* rank, int32_t* perm, const int64_t* t_off_out,
+                           void* t_out, cudaStream_t st) {
   const int ndim = (op == SKF_LAPLACE_2D || op == SKF_HELMHOLTZ_2D) ? 2 : 3;
   const bool geom_op = op >= SKF_LAPLACE_DOUBLE_LAYER_3D;
   const bool cplx = op == SKF_HELMHOLTZ_2D || op == SKF_HELMHOLTZ_3D || op == SKF_HELMHOLTZ_DOUBLE_LAYER_3D ||
@@ -450,9 +627,19 @@ int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double*
   const int mrows = geom_op ? 2 * np : np;
   std::vector<int64_t> hoff(nbox + 1);
   SKF_CUDA_TRY(cudaMemcpyAsync(hoff.data(), off, sizeof(int64_t) * (nbox + 1), cudaMemcpyDeviceToHost, st));
+  std::vector<int32_t> hk;
+  if (ra.kpred) {
+    hk.resize(nbox);
+    SKF_CUDA_TRY(cudaMemcpyAsync(hk.data(), ra.kpred, sizeof(int32_t) * nbox, cudaMemcpyDeviceToHost, st));
+  }
   SKF_CUDA_TRY(cudaStreamSynchronize(st));
-  int maxn = 1;
-  for (int b = 0; b < nbox; ++b) maxn = std::max<int>(maxn, (int)(hoff[b + 1] - hoff[b]));
+  // workspace rows per box: K, plus the sketch when the box is randomized
+  auto box_rows = [&](int b) -> int64_t {
+    const int64_t n = hoff[b + 1] - hoff[b];
+    if (!ra.kpred || hk[b] <= 0) return mrows;
+    const int64_t s = (int64_t)hk[b] + ra.oversample;
+    return (2 * s <= mrows && hk[b] < n) ? mrows + mrows / 2 : mrows;  // K and the largest sketch
+  };
 
   double* dtmpl = nullptr;
   SKF_CUDA_TRY(cudaMallocAsync(&dtmpl, sizeof(double) * tmpl.size(), st));
@@ -467,28 +654,47 @@ int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double*
     int64_t acc = 0;
     int b1 = b0;
     while (b1 < nbox) {
-      const int64_t need = (int64_t)mrows * (hoff[b1 + 1] - hoff[b1]) * W * (int64_t)sizeof(double);
+      const int64_t need = box_rows(b1) * (hoff[b1 + 1] - hoff[b1]) * W * (int64_t)sizeof(double);
       if (b1 > b0 && acc + need > budget) break;
       wso.push_back(acc / (int64_t)sizeof(double));
       acc += need;
       ++b1;
     }
+    // longest box first (cost ~ rows x n x min(rows, n)) so the tail of the
+    // launch holds the small boxes
+    std::vector<int32_t> ord(b1 - b0);
+    std::vector<double> cost(b1 - b0);
+    for (int b = b0; b < b1; ++b) {
+      const double n = (double)(hoff[b + 1] - hoff[b]);
+      double rows = mrows;
+      if (ra.kpred && hk[b] > 0 && 2 * ((int64_t)hk[b] + ra.oversample) <= mrows && hk[b] < n)
+        rows = (double)hk[b] + ra.oversample;
+      cost[b - b0] = rows * n * std::min(rows, n);
+      ord[b - b0] = b - b0;
+    }
+    std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
     double* ws = nullptr;
     int64_t* dwso = nullptr;
+    int32_t* dord = nullptr;
     cudaError_t e = cudaMallocAsync(&ws, std::max<int64_t>(acc, 8), st);
     if (e == cudaSuccess) e = cudaMallocAsync(&dwso, sizeof(int64_t) * wso.size(), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dord, sizeof(int32_t) * ord.size(), st);
     if (e != cudaSuccess) {
       set_last_cuda_error(e);
       status = SKF_ERR_OOM;
       if (ws) cudaFreeAsync(ws, st);
+      if (dwso) cudaFreeAsync(dwso, st);
       break;
     }
     e = cudaMemcpyAsync(dwso, wso.data(), sizeof(int64_t) * wso.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dord, ord.data(), sizeof(int32_t) * ord.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) {
       set_last_cuda_error(e);
       status = SKF_ERR_CUDA;
     }
-    SkelArgs a;
+    SkelArgs a{};
+    a.order = dord;
     a.off = off;
     a.x = x;
     a.geom = geom;
@@ -506,12 +712,30 @@ int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double*
     a.t_off_out = t_off_out;
     a.t_out = static_cast<double*>(t_out);
     a.first_box = b0;
+    a.kpred = ra.kpred;
+    a.oversample = ra.oversample;
+    a.rho = ra.rho;
+    a.seed = ra.seed;
+    a.nchk = ra.nchk;
+    a.sketch_tol = ra.sketch_tol;
+    a.resid_tol = ra.resid_tol;
+    a.resid = ra.resid;
+    a.status = ra.status;
     int maxn_batch = 1;
-    for (int b = b0; b < b1; ++b) maxn_batch = std::max<int>(maxn_batch, (int)(hoff[b + 1] - hoff[b]));
+    int64_t ymax = 0;
+    for (int b = b0; b < b1; ++b) {
+      const int64_t n = hoff[b + 1] - hoff[b];
+      maxn_batch = std::max<int>(maxn_batch, (int)n);
+      if (ra.kpred && hk[b] > 0 && 2 * ((int64_t)hk[b] + ra.oversample) <= mrows && hk[b] < n)
+        ymax = std::max<int64_t>(ymax, ((int64_t)hk[b] + ra.oversample) * n * W);
+    }
+    // first sketches in shared memory while they are small enough (<= 16 KB)
+    // to keep four blocks per SM
+    a.ycap = ymax <= 2048 ? ymax : 0;
     if (status == SKF_OK) {
       switch (op) {
 #define SKF_CASE(OPID) \
-  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, st); break;
+  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, mrows, st); break;
         SKF_CASE(SKF_LAPLACE_2D)
         SKF_CASE(SKF_LAPLACE_3D)
         SKF_CASE(SKF_HELMHOLTZ_2D)
@@ -526,12 +750,39 @@ int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double*
     }
     cudaFreeAsync(ws, st);
     cudaFreeAsync(dwso, st);
+    cudaFreeAsync(dord, st);
     b0 = b1;
   }
   cudaFreeAsync(dtmpl, st);
   if (status == SKF_OK) SKF_CUDA_TRY(cudaGetLastError());
-  (void)maxn;
   return status;
+}
+
+int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
+               const double* centers, double box_length, int nproxy, double tol, int32_t* rank, int32_t* perm,
+               const int64_t* t_off_out, void* t_out, cudaStream_t st) {
+  RandomizedArgs ra;
+  return skel_boxes_impl(op, kappa, nbox, off, x, geom, centers, box_length, nproxy, tol, ra, rank, perm, t_off_out,
+                         t_out, st);
+}
+
+int skel_boxes_randomized(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
+                          const double* centers, double box_length, int nproxy, double tol, const int32_t* kpred,
+                          int oversample, int rho, uint64_t seed, int nchk, double sketch_tol, double resid_tol,
+                          double* resid, int8_t* status, int32_t* rank, int32_t* perm, const int64_t* t_off_out,
+                          void* t_out, cudaStream_t st) {
+  RandomizedArgs ra;
+  ra.kpred = kpred;
+  ra.oversample = oversample;
+  ra.rho = rho;
+  ra.seed = seed;
+  ra.nchk = nchk;
+  ra.sketch_tol = sketch_tol;
+  ra.resid_tol = resid_tol;
+  ra.resid = resid;
+  ra.status = status;
+  return skel_boxes_impl(op, kappa, nbox, off, x, geom, centers, box_length, nproxy, tol, ra, rank, perm, t_off_out,
+                         t_out, st);
 }
 
 // Same work as skel_boxes, with the proxy template, the per-box workspace
@@ -581,7 +832,7 @@ int skel_boxes_scratch(int op, double kappa, int nbox, const int64_t* off, const
     // pageable source: the copy is staged before this call returns, and it is
     // ordered after the previous batch's kernel on the stream
     SKF_CUDA_TRY(cudaMemcpyAsync(dwso, wso.data(), sizeof(int64_t) * wso.size(), cudaMemcpyHostToDevice, st));
-    SkelArgs a;
+    SkelArgs a{};
     a.off = off;
     a.x = x;
     a.geom = geom;
@@ -603,7 +854,7 @@ int skel_boxes_scratch(int op, double kappa, int nbox, const int64_t* off, const
     for (int b = b0; b < b1; ++b) maxn_batch = std::max<int>(maxn_batch, (int)(hoff[b + 1] - hoff[b]));
     switch (op) {
 #define SKF_CASE(OPID) \
-  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, st); break;
+  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, mrows, st); break;
       SKF_CASE(SKF_LAPLACE_2D)
       SKF_CASE(SKF_LAPLACE_3D)
       SKF_CASE(SKF_HELMHOLTZ_2D)

@@ -24,6 +24,15 @@ int kernel_apply(int op, double kappa, int npairs, int mmax, int nmax, const int
 int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
                const double* centers, double box_length, int nproxy, double tol, int32_t* rank, int32_t* perm,
                const int64_t* t_off_out, void* t_out, cudaStream_t st);
+int skel_boxes_randomized(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
+                          const double* centers, double box_length, int nproxy, double tol, const int32_t* kpred,
+                          int oversample, int rho, uint64_t seed, int nchk, double sketch_tol, double resid_tol,
+                          double* resid, int8_t* status, int32_t* rank, int32_t* perm, const int64_t* t_off_out,
+                          void* t_out, cudaStream_t st);
+int proxy_rows(int op, int nproxy);
+int convert_f64_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
+int copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_off, const int64_t* len,
+                  const void* src, void* dst, int elem_bytes, cudaStream_t st);
 
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
@@ -187,17 +196,22 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   const int64_t tl = std::max<int64_t>(d->t_len, 1);
   SKF_TRY(upload(p, &p->t64, (const double*)nullptr, (size_t)tl * W));
   if (d->t_len > 0) {
-    cudaError_t e = cudaMemcpy(p->t64, d->t_data, sizeof(double) * d->t_len * W, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy(p->t64, d->t_data, sizeof(double) * d->t_len * W,
+                               d->t_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
       set_last_cuda_error(e);
       free_plan(p);
       return SKF_ERR_CUDA;
     }
   }
+  // FP32 copy of T, converted on the device
+  SKF_TRY(upload(p, &p->t32, (const float*)nullptr, (size_t)tl * W));
   {
-    std::vector<float> t32((size_t)tl * W, 0.f);
-    for (int64_t i = 0; i < d->t_len * W; ++i) t32[i] = (float)d->t_data[i];
-    SKF_TRY(upload(p, &p->t32, t32.data(), (size_t)tl * W));
+    const int st = convert_f64_f32(p->t64, p->t32, (int64_t)tl * W, nullptr);
+    if (st != SKF_OK) {
+      free_plan(p);
+      return st;
+    }
   }
   SKF_TRY(upload(p, &p->list_off, d->list_off, (size_t)nb + 1));
   SKF_TRY(upload(p, &p->list_src, d->list_src, (size_t)std::max<int64_t>(L, 1)));
@@ -448,6 +462,7 @@ int skf_kernel_apply(int32_t op, double kappa, int32_t npairs, int32_t mmax, int
   if (op < 0 || op >= SKF_NUM_OPS || npairs < 0 || mmax < 0 || nmax < 0) return SKF_ERR_ARG;
   if (npairs == 0 || mmax == 0) return SKF_OK;
   if (!m || !n || !xt || !xs || !q || !out) return SKF_ERR_ARG;
+  if ((mmax + 127) / 128 > 65535) return SKF_ERR_ARG;  // row tiles run on gridDim.y
   if (op_needs_geom(op) && ((op == SKF_LAPLACE_DOUBLE_LAYER_3D || op == SKF_HELMHOLTZ_DOUBLE_LAYER_3D) ? !gs : !gt))
     return SKF_ERR_ARG;
   if (precision != SKF_PREC_FP64 && precision != SKF_PREC_MIXED) return SKF_ERR_ARG;
@@ -464,6 +479,37 @@ int skf_skel_boxes(int32_t op, double kappa, int32_t nbox, const int64_t* off, c
   if (op_needs_geom(op) && !geom) return SKF_ERR_ARG;
   return skel_boxes(op, kappa, nbox, off, x, geom, centers, box_length, nproxy, tol, rank, perm, t_off_out, t_out,
                     static_cast<cudaStream_t>(stream));
+}
+
+int skf_copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_off, const int64_t* len,
+                      const void* src, void* dst, int32_t elem_bytes, void* stream) {
+  if (nseg < 0 || (elem_bytes != 8 && elem_bytes != 16)) return SKF_ERR_ARG;
+  if (nseg == 0) return SKF_OK;
+  if (!src_off || !dst_off || !len || !src || !dst) return SKF_ERR_ARG;
+  return copy_segments(nseg, src_off, dst_off, len, src, dst, elem_bytes, static_cast<cudaStream_t>(stream));
+}
+
+int skf_proxy_rows(int32_t op, int32_t nproxy, int32_t* rows_out) {
+  if (op < 0 || op >= SKF_NUM_OPS || nproxy <= 0 || !rows_out) return SKF_ERR_ARG;
+  *rows_out = proxy_rows(op, nproxy);
+  return SKF_OK;
+}
+
+int skf_skel_boxes_randomized(int32_t op, double kappa, int32_t nbox, const int64_t* off, const double* x,
+                              const double* geom, const double* centers, double box_length, int32_t nproxy,
+                              double tol, const int32_t* kpred, int32_t oversample, int32_t rho, uint64_t seed,
+                              int32_t nchk, double sketch_tol, double resid_tol, double* resid, int8_t* status,
+                              int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out, void* stream) {
+  if (op < 0 || op >= SKF_NUM_OPS || nbox < 0 || nproxy <= 0 || !(box_length > 0) || !(tol > 0) || !(tol < 1))
+    return SKF_ERR_ARG;
+  if (oversample < 2 || rho < 1 || nchk < 0 || !(resid_tol >= 0) || !(sketch_tol > 0) || !(sketch_tol < 1))
+    return SKF_ERR_ARG;
+  if (nbox == 0) return SKF_OK;
+  if (!off || !x || !centers || !rank || !perm || !t_off_out || !t_out || !kpred) return SKF_ERR_ARG;
+  if (op_needs_geom(op) && !geom) return SKF_ERR_ARG;
+  return skel_boxes_randomized(op, kappa, nbox, off, x, geom, centers, box_length, nproxy, tol, kpred, oversample, rho,
+                               seed, nchk, sketch_tol, resid_tol, resid, status, rank, perm, t_off_out, t_out,
+                               static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(128, 5) k_translate_sym(SymArgs a) {
 }
 
 // Adds the B-side partial sums into u / uh in a fixed order.  Block
-// (chunk, box): entries [256 chunk, 256 chunk + 256) of the box.
+// (box, chunk): entries [256 chunk, 256 chunk + 256) of the box.
 template <bool LOG>
 __global__ void __launch_bounds__(256) k_sym_reduce(const int64_t* __restrict__ box_off,
                                                     const int32_t* __restrict__ box_rank,
@@ -858,10 +858,10 @@ __global__ void __launch_bounds__(256) k_sym_reduce(const int64_t* __restrict__ 
                                                     const int64_t* __restrict__ in_blk,
                                                     const float* __restrict__ pbuf, double* __restrict__ u,
                                                     double* __restrict__ uh) {
-  const int B = blockIdx.y;
+  const int B = blockIdx.x;
   const int64_t off = box_off[B];
   const int bs = (int)(box_off[B + 1] - off);
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
   const int64_t k0 = in_off[B], k1 = in_off[B + 1];
   if (j >= bs || k0 == k1) return;
   const int r = box_rank[B];

@@ -15,6 +15,7 @@ import ctypes
 from dataclasses import dataclass
 
 import numpy as np
+import torch
 
 from . import _lib
 from .operators import cuda_op_id, is_complex_op
@@ -181,8 +182,18 @@ class Plan:
         d.perm_entry = arr("perm_entry", rb.perm_entry, np.int64)
         d.perm_point = arr("perm_point", rb.perm_point, np.int64)
         d.t_off = arr("t_off", rb.t_off, np.int64)
-        tdt = np.complex128 if self.is_complex else np.float64
-        d.t_data = arr("t_data", rb.t_data, tdt)
+        if isinstance(rb.t_data, torch.Tensor):
+            # T blocks already on the device: copied device to device
+            tdt = torch.complex128 if self.is_complex else torch.float64
+            if not rb.t_data.is_cuda or rb.t_data.dtype != tdt or not rb.t_data.is_contiguous():
+                raise ValueError("device t_data must be a contiguous CUDA tensor of the operator's dtype")
+            keep["t_data"] = rb.t_data
+            d.t_data = rb.t_data.data_ptr()
+            d.t_on_device = 1
+        else:
+            tdt = np.complex128 if self.is_complex else np.float64
+            d.t_data = arr("t_data", rb.t_data, tdt)
+            d.t_on_device = 0
         d.t_len = int(rb.t_data.shape[0])
         d.list_off = arr("list_off", rb.list_off, np.int64)
         d.list_src = arr("list_src", rb.list_src, np.int32)

@@ -36,8 +36,42 @@ def nproxy_levels(ndim, tol, kappa, L0, nlevels):
     return out
 
 
+def _concat_ranges(starts, lens):
+    """Concatenation of the integer ranges [starts[i], starts[i] + lens[i])."""
+    lens = np.asarray(lens, dtype=np.int64)
+    total = int(lens.sum())
+    if total == 0:
+        return np.zeros(0, dtype=np.int64)
+    before = np.cumsum(lens) - lens
+    return np.arange(total, dtype=np.int64) + np.repeat(np.asarray(starts, dtype=np.int64) - before, lens)
+
+
+class _BoxView:
+    """``view[b]`` -> per-box slice of level-flat storage (read only)."""
+
+    def __init__(self, nboxes, getter):
+        self._n = nboxes
+        self._get = getter
+
+    def __len__(self):
+        return self._n
+
+    def __getitem__(self, b):
+        return self._get(int(b))
+
+    def __iter__(self):
+        return (self._get(b) for b in range(self._n))
+
+
 class RecursiveSkeletonization:
-    """Build of the skeletonized tree for one operator (GPU IDs)."""
+    """Build of the skeletonized tree for one operator (GPU IDs).
+
+    Storage is level-flat: ``_ids[lev]`` holds the point ids of every box of
+    level ``lev`` back to back (box ``b`` at ``_off[lev][b - level_sep[lev]]``),
+    in skeleton-first order once the level is skeletonized; the T blocks of a
+    level stay on the device in ``_tdev[lev]`` (row-major r x (bs - r) per
+    box at ``_toff[lev]``).
+    """
 
     def __init__(self, tree, operator, kappa, tol, max_bs=-1, max_rank=-1, geometry=None, device=None):
         self.N = tree.N
@@ -60,77 +94,213 @@ class RecursiveSkeletonization:
         if self.device.type != "cuda":
             raise RuntimeError("the skeletonization build runs on a CUDA device")
 
-        leaves = tree.get_leaves()
         self.nproxy_level = nproxy_levels(self.ndim, tol, self.kappa, tree.L0, self.nlevels)
         self.max_bs_leaf = tree.leaf_size
+        if np.any(tree.get_box_npoints(tree.get_leaves()) > self.max_bs_leaf):
+            raise ValueError("Leaf block size exceeds maximum allowed")
         self.bs_list = np.zeros(self.nboxes, dtype=np.int64)
         self.rank_list = np.zeros(self.nboxes, dtype=np.int64)
-        self.pid = [None] * self.nboxes
-        self.proj = [None] * self.nboxes  # host copies of T (rank x (bs-rank))
-        for leaf in leaves:
-            inds = tree.get_box_inds(leaf)
-            if inds.shape[0] > self.max_bs_leaf:
-                raise ValueError("Leaf block size exceeds maximum allowed")
-            self.pid[leaf] = np.asarray(inds, dtype=np.int64)
-            self.bs_list[leaf] = inds.shape[0]
-        self.root_level = max(0, self.nlevels - 1)
+        leaves = tree.get_leaves()
+        self.bs_list[leaves] = tree.get_box_npoints(leaves)
+        nl = self.nlevels
+        self._ids = [None] * nl
+        self._off = [None] * nl
+        self._cand_src = [None] * nl   # candidate -> child-level entry (or -1)
+        self._final_pos = [None] * nl  # candidate -> entry position after the ID
+        self._tdev = [None] * nl
+        self._toff = [None] * nl
+        self.root_level = max(0, nl - 1)
         self.level_times = {}
+        self.level_stats = {}
+        self._resid_by_lev = {}
+        # optional callable(fmm, lev, boxes, x_lev, off) -> predicted ranks (int64,
+        # -1 = no prediction): enables the sampled (randomized) IDs
+        self.rank_predictor = None
+        self.oversample = 10   # sketch rows beyond the predicted rank
+        self.rho = 16          # nonzeros per sketch row
+        self.nchk = 16         # proxy rows of the residual check
+        self.sketch_factor = 0.25  # rank rule on the sketch: |R_kk| <= factor * tol * |R_00|
+        self.resid_factor = 1.0  # keep the randomized ID when residual <= factor * tol
+        self.seed = 12345
         self._XX_dev = torch.from_numpy(np.ascontiguousarray(tree.XX)).to(self.device)
+        self._geom_dev = None
+        if self.geometry is not None:
+            self._geom_dev = torch.from_numpy(self.geometry).to(self.device)
+        self.pid = _BoxView(self.nboxes, self._box_ids)
+        self.proj = _BoxView(self.nboxes, self._box_proj)
 
     @property
     def rank_max(self):
         pos = self.rank_list[self.rank_list > 0]
         return int(pos.max()) if pos.size else 0
 
-    def _update_lev_skel(self, lev):
-        """Parent candidate set = children's skeletons (recursive_skel.py:209-262)."""
-        for box in self.tree.get_boxes_level(lev):
-            if self.tree.is_leaf(box):
-                continue
-            parts = [self.pid[c][: self.rank_list[c]] for c in self.tree.get_box_children(box)]
-            self.pid[box] = np.concatenate(parts) if parts else np.zeros(0, np.int64)
-            self.bs_list[box] = self.pid[box].shape[0]
+    # ------------------------------------------------------------ views
+    def _box_ids(self, b):
+        lev = int(self.tree._box_level[b])
+        if self._ids[lev] is None:
+            if self.tree.is_leaf(b):
+                return np.asarray(self.tree.get_box_inds(b), dtype=np.int64)
+            return None
+        i = b - int(self.tree.level_sep[lev])
+        o = self._off[lev]
+        return self._ids[lev][o[i]:o[i + 1]]
+
+    def _box_proj(self, b):
+        lev = int(self.tree._box_level[b])
+        if self._tdev[lev] is None:
+            return None
+        i = b - int(self.tree.level_sep[lev])
+        r, s = int(self.rank_list[b]), int(self.bs_list[b])
+        t0 = int(self._toff[lev][i])
+        return self._tdev[lev][t0:t0 + r * (s - r)].cpu().numpy().reshape(r, s - r)
+
+    # ------------------------------------------------------------ levels
+    def _level_candidates(self, lev):
+        """Entries of every box at ``lev`` before its ID: the points of a
+        leaf, else the skeletons of its children in child order
+        (recursive_skel.py:209-262)."""
+        tree = self.tree
+        ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+        boxes = np.arange(ls, le, dtype=np.int64)
+        leaf = tree._is_leaf[boxes]
+        lb = boxes[leaf]
+        seg_box = [lb]
+        seg_start = [tree._box_start[lb]]
+        seg_len = [tree._box_end[lb] - tree._box_start[lb]]
+        seg_child = [np.full(lb.shape[0], -1, dtype=np.int64)]
+        if lev + 1 < self.nlevels and self._ids[lev + 1] is not None:
+            nlb = boxes[~leaf]
+            ch = tree._children[nlb]
+            mask = ch >= 0
+            cb = np.repeat(nlb, ch.shape[1]).reshape(ch.shape)[mask]
+            cc = ch[mask]
+            cl = cc - int(tree.level_sep[lev + 1])
+            seg_box.append(cb)
+            seg_start.append(self.N + self._off[lev + 1][cl])
+            seg_len.append(self.rank_list[cc])
+            seg_child.append(cc)
+        sb = np.concatenate(seg_box)
+        order = np.argsort(sb, kind="stable")
+        sb = sb[order]
+        st = np.concatenate(seg_start)[order]
+        sl = np.concatenate(seg_len)[order].astype(np.int64)
+        idx = _concat_ranges(st, sl)
+        src = np.concatenate((tree._perm.astype(np.int64),
+                              self._ids[lev + 1] if (lev + 1 < self.nlevels and self._ids[lev + 1] is not None)
+                              else np.zeros(0, np.int64)))
+        ids = src[idx]
+        bs = np.bincount(sb - ls, weights=sl, minlength=le - ls).astype(np.int64)
+        off = np.zeros(le - ls + 1, dtype=np.int64)
+        np.cumsum(bs, out=off[1:])
+        self._ids[lev] = ids
+        self._off[lev] = off
+        self._cand_src[lev] = np.where(idx >= self.N, idx - self.N, -1)
+        self._final_pos[lev] = None
+        self.bs_list[ls:le] = bs
+
+    def _leaf_level_entries(self, lev):
+        """Entries of a level above the root: leaves hold their points."""
+        self._level_candidates(lev)
 
     def _skel_level(self, lev):
-        """Proxy IDs of every box at ``lev`` in one GPU call."""
+        """Proxy IDs of every box at ``lev`` on the GPU in one call.  With a
+        rank predictor, every box whose predicted rank is below its size
+        first tries the randomized ID at that rank (sparse-sign sketch of
+        predicted rank + oversampling rows), kept when its residual on
+        held-out rows of the proxy matrix is within tol, else the full
+        pivoted-QR ID (decided per box inside the kernel)."""
         tree = self.tree
-        boxes = tree.get_boxes_level(lev)
-        bs = self.bs_list[boxes]
-        off = np.zeros(boxes.shape[0] + 1, dtype=np.int64)
-        np.cumsum(bs, out=off[1:])
-        ids = np.concatenate([self.pid[b] for b in boxes]) if off[-1] > 0 else np.zeros(0, np.int64)
         dev = self.device
+        ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+        nbl = le - ls
+        off = self._off[lev]
+        bs = np.diff(off)
+        ids = self._ids[lev]
         ids_t = torch.from_numpy(ids).to(dev)
         x = self._XX_dev.index_select(0, ids_t).contiguous()
         g = None
-        if self.geometry is not None:
-            g = torch.from_numpy(self.geometry).to(dev).index_select(0, ids_t).contiguous()
-        centers = torch.from_numpy(np.ascontiguousarray(tree.get_boxes_centers(boxes))).to(dev)
+        if self._geom_dev is not None:
+            g = self._geom_dev.index_select(0, ids_t).contiguous()
+        centers = torch.from_numpy(np.ascontiguousarray(tree._box_center[ls:le])).to(dev)
         cplx = is_complex_op(self.op_id)
         cap = (bs * bs) // 4 + bs
-        t_off = np.zeros(boxes.shape[0], dtype=np.int64)
+        t_off = np.zeros(nbl, dtype=np.int64)
         np.cumsum(cap[:-1], out=t_off[1:])
-        t_len = int(cap.sum())
-        t_buf = torch.zeros(max(t_len, 1), dtype=torch.complex128 if cplx else torch.float64, device=dev)
-        rank = torch.zeros(boxes.shape[0], dtype=torch.int32, device=dev)
+        tdt = torch.complex128 if cplx else torch.float64
+        t_buf = torch.zeros(max(int(cap.sum()), 1), dtype=tdt, device=dev)
+        rank = torch.zeros(nbl, dtype=torch.int32, device=dev)
         perm = torch.zeros(max(int(off[-1]), 1), dtype=torch.int32, device=dev)
         off_t = torch.from_numpy(off).to(dev)
         t_off_t = torch.from_numpy(t_off).to(dev)
-        stream = torch.cuda.current_stream(dev).cuda_stream
-        _lib.check(_lib.load().skf_skel_boxes(
-            self.op_id, self.kappa, int(boxes.shape[0]), _lib.ptr(off_t), _lib.ptr(x), _lib.ptr(g),
-            _lib.ptr(centers), float(tree.get_box_length(boxes[0])), int(self.nproxy_level[lev]),
-            float(self.tol), _lib.ptr(rank), _lib.ptr(perm), _lib.ptr(t_off_t), _lib.ptr(t_buf),
-            ctypes.c_void_p(stream)), "skf_skel_boxes")
+        stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        lib = _lib.load()
+        length = float(tree.L0 * 0.5 ** lev)
+        mrows = self._mrows(lev)
+        stats = {"boxes": nbl, "rows_full": int(mrows)}
+        pred = None
+        if self.rank_predictor is not None and self.tol < 1:
+            t0 = perf_counter()
+            pred = np.asarray(self.rank_predictor(self, lev, np.arange(ls, le), x, off), dtype=np.int64)
+            stats["predict_s"] = perf_counter() - t0
+        if pred is None:
+            _lib.check(lib.skf_skel_boxes(
+                self.op_id, self.kappa, nbl, _lib.ptr(off_t), _lib.ptr(x), _lib.ptr(g), _lib.ptr(centers), length,
+                int(self.nproxy_level[lev]), float(self.tol), _lib.ptr(rank), _lib.ptr(perm), _lib.ptr(t_off_t),
+                _lib.ptr(t_buf), stream), "skf_skel_boxes")
+            stats.update(randomized=0, kept=0, fallback=0)
+        else:
+            kpred = np.where((pred > 0) & (pred < bs), pred, 0).astype(np.int32)
+            kpred_t = torch.from_numpy(kpred).to(dev)
+            resid = torch.empty(nbl, dtype=torch.float64, device=dev)
+            status = torch.empty(nbl, dtype=torch.int8, device=dev)
+            _lib.check(lib.skf_skel_boxes_randomized(
+                self.op_id, self.kappa, nbl, _lib.ptr(off_t), _lib.ptr(x), _lib.ptr(g), _lib.ptr(centers), length,
+                int(self.nproxy_level[lev]), float(self.tol), _lib.ptr(kpred_t), int(self.oversample), int(self.rho),
+                int(self.seed + lev), int(self.nchk), float(self.sketch_factor * self.tol),
+                float(self.resid_factor * self.tol), _lib.ptr(resid),
+                _lib.ptr(status), _lib.ptr(rank), _lib.ptr(perm), _lib.ptr(t_off_t), _lib.ptr(t_buf), stream),
+                "skf_skel_boxes_randomized")
+            st = status.cpu().numpy()
+            self._last_resid = resid.cpu().numpy()
+            self._resid_by_lev[lev] = self._last_resid
+            rounds = st // 10
+            stats.update(randomized=int(np.count_nonzero(st > 0)), kept=int(np.count_nonzero(st % 10 == 1)),
+                         fallback=int(np.count_nonzero(st % 10 == 2)), sketch_rounds=int(rounds.sum()),
+                         sketch_rows=int(np.sum(np.where(st > 0, (kpred + self.oversample) * (2 ** rounds - 1), 0))))
+            self._last_pred = pred
+            self._last_status = st
         rank_h = rank.cpu().numpy().astype(np.int64)
-        perm_h = perm.cpu().numpy().astype(np.int64)
-        t_h = t_buf.cpu().numpy()
-        for i, b in enumerate(boxes):
-            r, s = int(rank_h[i]), int(bs[i])
-            p = perm_h[off[i]: off[i + 1]]
-            self.rank_list[b] = r
-            self.pid[b] = self.pid[b][p]
-            self.proj[b] = t_h[t_off[i]: t_off[i] + r * (s - r)].reshape(r, s - r)
+        perm_h = perm.cpu().numpy().astype(np.int64)[: int(off[-1])]
+        self.level_stats[lev] = stats
+        # skeleton-first ids, candidate -> final position
+        base = np.repeat(off[:-1], bs)
+        src = base + perm_h
+        self._ids[lev] = ids[src]
+        fp = np.empty(ids.shape[0], dtype=np.int64)
+        fp[src] = np.arange(ids.shape[0], dtype=np.int64)
+        self._final_pos[lev] = fp
+        self.rank_list[ls:le] = rank_h
+        # compact the T blocks
+        tl = rank_h * (bs - rank_h)
+        toff = np.zeros(nbl + 1, dtype=np.int64)
+        np.cumsum(tl, out=toff[1:])
+        tc = torch.empty(max(int(toff[-1]), 1), dtype=tdt, device=dev)
+        nz = np.flatnonzero(tl > 0)
+        if nz.size:
+            so = torch.from_numpy(t_off[nz]).to(dev)
+            do = torch.from_numpy(toff[:-1][nz]).to(dev)
+            ln = torch.from_numpy(tl[nz]).to(dev)
+            _lib.check(lib.skf_copy_segments(int(nz.size), _lib.ptr(so), _lib.ptr(do), _lib.ptr(ln), _lib.ptr(t_buf),
+                                             _lib.ptr(tc), 16 if cplx else 8, stream), "skf_copy_segments")
+        self._tdev[lev] = tc
+        self._toff[lev] = toff[:-1]
+        del t_buf
+
+    def _mrows(self, lev):
+        out = ctypes.c_int32()
+        _lib.check(_lib.load().skf_proxy_rows(self.op_id, int(self.nproxy_level[lev]), ctypes.byref(out)),
+                   "skf_proxy_rows")
+        return int(out.value)
 
     def skel_tree(self, npoints_max, p=None, verbose=False):
         """Level loop of recursive_skel.py:326-502 with GPU IDs per level.
@@ -140,10 +310,10 @@ class RecursiveSkeletonization:
         tree = self.tree
         self.root_level = max(0, tree.nlevels - 1)
         for lev in range(tree.nlevels - 1, 0, -1):
-            self._update_lev_skel(lev)
+            self._level_candidates(lev)
             boxes_lev = tree.get_boxes_level(lev)
-            active = np.hstack((tree.get_leaves_above(lev), boxes_lev)).astype(np.int64)
-            npoints_lev = int(np.sum(self.bs_list[active]))
+            above = tree.get_leaves_above(lev)
+            npoints_lev = int(np.sum(self.bs_list[boxes_lev]) + np.sum(self.bs_list[above]))
             if verbose:
                 print("\t Level %2d has %6d npoints" % (lev, npoints_lev))
             if lev == 2 or npoints_lev <= npoints_max:
@@ -155,6 +325,10 @@ class RecursiveSkeletonization:
             self.level_times[lev] = perf_counter() - t0
             if verbose:
                 print("\t Level %2d ids: %5.3f s" % (lev, self.level_times[lev]))
+        if tree.nlevels == 1:
+            self._level_candidates(0)
+        for lev in range(self.root_level - 1, -1, -1):
+            self._leaf_level_entries(lev)
         return self
 
     def setup_lists(self, verbose=False):
@@ -163,7 +337,7 @@ class RecursiveSkeletonization:
         tree = self.tree
         nb = self.nboxes
         levels = tree.get_boxes_levels()
-        leaf_mask = tree.are_leaves(np.arange(nb))
+        leaf_mask = tree._is_leaf
         below = levels > self.root_level
         boxes_below = np.flatnonzero(below)
         col = tree.get_boxes_colleague_neigh_fullvec(boxes_below)
@@ -186,51 +360,61 @@ class RecursiveSkeletonization:
             (_lib.KIND_COLLEAGUE, coll), (_lib.KIND_COARSE_UP, up),
             (_lib.KIND_COARSE_DOWN, up[:, ::-1]), (_lib.KIND_ROOT, root)])
 
-        # entries and offsets
-        bs = np.array([0 if p is None else p.shape[0] for p in self.pid], dtype=np.int64)
+        # entries: levels in order, boxes in order (levels above the root:
+        # leaves only)
+        bs = np.zeros(nb, dtype=np.int64)
+        ids_all, ebase = [], np.zeros(self.nlevels + 1, dtype=np.int64)
+        for lev in range(self.nlevels):
+            ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+            if self._ids[lev] is None:
+                ebase[lev + 1] = ebase[lev]
+                continue
+            bl = np.diff(self._off[lev])
+            if lev < self.root_level:
+                bl = np.where(leaf_mask[ls:le], bl, 0)
+                keep = np.repeat(leaf_mask[ls:le], np.diff(self._off[lev]))
+                ids_all.append(self._ids[lev][keep])
+            else:
+                ids_all.append(self._ids[lev])
+            bs[ls:le] = bl
+            ebase[lev + 1] = ebase[lev] + int(bl.sum())
         self.bs_list = bs
         off = np.zeros(nb + 1, dtype=np.int64)
         np.cumsum(bs, out=off[1:])
         self.box_off = off
-        ids = np.concatenate([self.pid[b] for b in range(nb) if bs[b] > 0])
+        ids = np.concatenate(ids_all) if ids_all else np.zeros(0, np.int64)
         self.entry_pid = ids
-        # parent slots of skeleton entries
+        # parent slots: skeleton entry i of child c sits at candidate position
+        # t of its parent, which the parent's ID moved to _final_pos
         pslot = np.full(int(off[-1]), -1, dtype=np.int64)
-        for lev in range(self.root_level, self.nlevels):
-            for box in tree.get_boxes_level(lev):
-                if leaf_mask[box]:
-                    continue
-                kids = tree.get_box_children(box)
-                rk = self.rank_list[kids]
-                if lev == self.root_level:
-                    pos = np.arange(int(rk.sum()))
-                else:
-                    cand = np.concatenate([self.pid[c][: self.rank_list[c]] for c in kids])
-                    order = np.argsort(self.pid[box])
-                    pos = order[np.searchsorted(self.pid[box], cand, sorter=order)]
-                acc = 0
-                for c, r in zip(kids, rk):
-                    pslot[off[c]: off[c] + r] = off[box] + pos[acc: acc + r]
-                    acc += r
+        for lev in range(self.root_level, self.nlevels - 1):
+            cs = self._cand_src[lev]
+            if cs is None:
+                continue
+            t = np.flatnonzero(cs >= 0)
+            fpos = t if self._final_pos[lev] is None else self._final_pos[lev][t]
+            pslot[ebase[lev + 1] + cs[t]] = ebase[lev] + fpos
         self.entry_pslot = pslot
-        leaves = tree.get_leaves()
-        self.perm_entry = np.concatenate([np.arange(off[b], off[b + 1]) for b in leaves])
-        self.perm_point = np.concatenate([self.pid[b] for b in leaves])
-        # T blocks
+        ent_leaf = np.repeat(leaf_mask, bs)
+        self.perm_entry = np.flatnonzero(ent_leaf).astype(np.int64)
+        self.perm_point = ids[self.perm_entry]
+        # T blocks: device buffers of the skeletonized levels, back to back
         cplx = is_complex_op(self.op_id)
         t_off = np.full(nb, -1, dtype=np.int64)
-        blocks = []
-        acc = 0
-        for b in range(nb):
-            r = int(self.rank_list[b])
-            if r <= 0 or levels[b] <= self.root_level or self.proj[b] is None:
+        parts, acc = [], 0
+        for lev in range(self.root_level + 1, self.nlevels):
+            if self._tdev[lev] is None:
                 continue
-            t_off[b] = acc
-            blocks.append(self.proj[b].ravel())
-            acc += self.proj[b].size
-        dt = np.complex128 if cplx else np.float64
+            ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+            r = self.rank_list[ls:le]
+            has = r > 0
+            t_off[ls:le] = np.where(has, self._toff[lev] + acc, -1)
+            used = int((r * (np.diff(self._off[lev]) - r)).sum())
+            parts.append(self._tdev[lev][:used] if used else self._tdev[lev][:0])
+            acc += used
+        dt = torch.complex128 if cplx else torch.float64
         self.t_off = t_off
-        self.t_data = np.concatenate(blocks).astype(dt) if blocks else np.zeros(1, dt)
+        self.t_data = torch.cat(parts) if acc else torch.zeros(1, dtype=dt, device=self.device)
         if verbose:
             print("\t root level %d, %d root boxes, %d entries" % (self.root_level, root_boxes.shape[0], off[-1]))
 

@@ -85,8 +85,11 @@ class SkelFMM:
 
     def __init__(self, points, operator, geometry=None, tol=1e-5, rank_or_tol=None, leaf_size=200,
                  use_single_precision=False, param=0.0, quiet=True, keep_host_fmm=False, defer_build=False,
-                 npoints_max=500, p="auto", max_bs=-1, max_rank=-1, precision=None):
+                 npoints_max=500, p="auto", max_bs=-1, max_rank=-1, precision=None, learned_rank=False):
         self.points = np.asarray(points, dtype=np.float64)
+        # learned_rank: False (pivoted-QR IDs, as the reference), True (packaged
+        # rank network), a path to weights, or a RankMLP
+        self.learned_rank = learned_rank
         self.operator = _require_operator(operator)
         self.geometry = geometry
         self.param = param
@@ -160,6 +163,12 @@ class SkelFMM:
             fmm = RecursiveSkeletonization(self.tree, self.operator, kappa=self.param, tol=self.rank_or_tol,
                                            max_bs=self._max_bs_limit, max_rank=self._max_rank_limit,
                                            geometry=self.geometry, device=self.device)
+            if self.learned_rank is not False and self.learned_rank is not None:
+                from .rank_model import DEFAULT_WEIGHTS, LearnedRankPredictor, RankMLP
+
+                lr = self.learned_rank
+                model = lr if isinstance(lr, RankMLP) else RankMLP.load(DEFAULT_WEIGHTS if lr is True else lr)
+                fmm.rank_predictor = LearnedRankPredictor(model)
             t0 = perf_counter()
             fmm.skel_tree(npoints_max=npoints_max, verbose=verbose)
             self.skel_time_seconds = perf_counter() - t0
@@ -172,7 +181,7 @@ class SkelFMM:
         self.rank_max = fmm.rank_max
         self.fmm = fmm if self._keep_host_fmm else None
         self.device_storage_bytes = int(self.plan.info.device_bytes)
-        self.host_build_storage_bytes = int(sum(p.nbytes for p in fmm.pid if p is not None))
+        self.host_build_storage_bytes = int(sum(a.nbytes for a in fmm._ids if a is not None))
         self.host_storage_bytes = self.host_build_storage_bytes if self._keep_host_fmm else 0
         self.total_storage_bytes = self.host_storage_bytes + self.device_storage_bytes
         self.nbytes = self.total_storage_bytes

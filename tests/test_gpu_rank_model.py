@@ -1,0 +1,163 @@
+"""Learned-rank build on the GPU: the BF16 rank network's kernels against the
+CPU oracle (oracle/mlp_oracle.py), its training, the randomized IDs with
+their residual check and pivoted-QR fallback, and what the trained network
+gains over the same build without it."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+NIN = 22
+
+
+def _model(seed=1):
+    from skelfmm_gb300.rank_model import RankMLP
+
+    return RankMLP(nin=NIN, seed=seed)
+
+
+def _data(n=300, seed=0):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, NIN)).astype(np.float32)
+    y = (np.sin(X[:, 0]) + 0.5 * X[:, 1] * X[:, 2] - 0.3 * np.abs(X[:, 3])).astype(np.float32)
+    return X, y
+
+
+def _oracle_inputs(m, X):
+    theta16 = m.theta16.float().cpu().numpy()
+    X16 = M.bf16_round(X)
+    return theta16, X16
+
+
+def test_mlp_gradient_matches_oracle():
+    m = _model()
+    X, y = _data()
+    loss, g = m.gradient(X, y)
+    theta16, X16 = _oracle_inputs(m, X)
+    lo, go = M.loss_and_grad(theta16, X16, y, NIN, bf16=True)
+    assert abs(loss - lo) <= 1e-3 * lo
+    # per-block relative error (BF16 activations may round differently at a
+    # few ties when the FP32 sums are taken in another order)
+    assert np.linalg.norm(g - go) <= 2e-2 * np.linalg.norm(go)
+    W1 = slice(0, 128 * NIN)
+    assert np.linalg.norm(g[W1] - go[W1]) <= 2e-2 * np.linalg.norm(go[W1])
+
+
+def test_mlp_predict_matches_oracle():
+    m = _model(seed=2)
+    X, _ = _data(n=257, seed=4)  # not a multiple of the 64-sample tile
+    y = m.predict(X)
+    theta16, X16 = _oracle_inputs(m, X)
+    _, _, _, yo = M.forward(theta16, X16, NIN, bf16=True)
+    assert np.max(np.abs(y - yo)) <= 1e-3 * max(1.0, np.max(np.abs(yo)))
+
+
+def test_adam_step_matches_oracle():
+    m = _model(seed=3)
+    X, y = _data(n=128, seed=5)
+    theta0 = m.theta.cpu().numpy().astype(np.float64)
+    _, g = m.gradient(X, y)
+    m.fit(X, y, steps=1, batch=10**9, lr=1e-3, lr_min=1e-3, normalise=False)
+    got = m.theta.cpu().numpy()
+    want = M.adam_step(theta0.copy(), np.zeros_like(theta0), np.zeros_like(theta0), g.astype(np.float64), 1, 1e-3)
+    # a bias-corrected first Adam step moves every weight by ~lr * sign(g)
+    assert np.max(np.abs(got - want)) <= 1e-5
+
+
+def test_training_reduces_loss():
+    m = _model(seed=4)
+    X, y = _data(n=4096, seed=6)
+    hist = m.fit(X, y, steps=600, batch=512, lr=3e-3, log_every=100)
+    first, last = hist[0][1], hist[-1][1]
+    assert last < 0.1 * first
+    pred = m.predict(X)
+    assert np.mean((pred - y) ** 2) < 0.1 * np.var(y)
+
+
+def _cube_build(rank_predictor=None, n=40000, leaf=64, seed=0):
+    from skelfmm_gb300 import operators
+    from skelfmm_gb300.plan import Plan
+    from skelfmm_gb300.recursive_skel import RecursiveSkeletonization
+    from skelfmm_gb300.tree import BalancedTree
+
+    pts = np.random.default_rng(seed).random((n, 3))
+    tree = BalancedTree(pts, leaf)
+    f = RecursiveSkeletonization(tree, operators.LAPLACE_3D, 0.0, 1e-6)
+    f.rank_predictor = rank_predictor
+    f.skel_tree(500)
+    f.setup_lists()
+    return pts, f, Plan(f.ragged())
+
+
+def _apply_error(pts, plan, nchk=300):
+    from skelfmm_gb300 import _lib, operators
+    from skelfmm_gb300.skel_fmm import direct_sum
+
+    x = np.random.RandomState(1).randn(pts.shape[0])
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.empty_like(xt)
+    plan.apply_device(xt, yt, _lib.PREC_FP64)
+    idx = np.random.default_rng(0).choice(pts.shape[0], nchk, replace=False)
+    yd = direct_sum(operators.LAPLACE_3D, pts, x, idx)
+    y = yt.cpu().numpy()
+    return float(np.abs(y[idx] - yd).max() / np.abs(yd).max())
+
+
+@pytest.fixture(scope="module")
+def reference_build():
+    pts, f, plan = _cube_build()
+    return pts, f, _apply_error(pts, plan)
+
+
+def test_learned_build_meets_tolerance(reference_build):
+    from skelfmm_gb300.rank_model import LearnedRankPredictor, RankMLP
+
+    pts, f_full, err_full = reference_build
+    _, f, plan = _cube_build(LearnedRankPredictor(RankMLP.load()))
+    kept = sum(s.get("kept", 0) for s in f.level_stats.values())
+    randomized = sum(s.get("randomized", 0) for s in f.level_stats.values())
+    assert randomized > 0 and kept >= 0.5 * randomized
+    err = _apply_error(pts, plan)
+    assert err <= max(3 * err_full, 1e-6), (err, err_full)
+    # ranks stay close to the pivoted-QR ranks (the sketch rule is tol / 4)
+    lv = f.tree.get_boxes_levels()
+    sk = lv > f.root_level
+    assert np.mean(f.rank_list[sk]) <= 1.15 * np.mean(f_full.rank_list[sk]) + 2
+
+
+def test_underpredicted_ranks_fall_back_to_pivoted_qr(reference_build):
+    pts, f_full, err_full = reference_build
+
+    class TooSmall:
+        def __call__(self, fmm, lev, boxes, x_lev, off):
+            return np.full(boxes.shape[0], 2, dtype=np.int64)
+
+    _, f, plan = _cube_build(TooSmall())
+    st = {k: v for k, v in f.level_stats.items()}
+    assert sum(s["randomized"] for s in st.values()) > 0
+    # tiny sketches saturate and double; the result still meets the tolerance
+    assert sum(s["sketch_rounds"] for s in st.values()) > sum(s["randomized"] for s in st.values())
+    assert _apply_error(pts, plan) <= max(3 * err_full, 1e-6)
+
+
+def test_network_gains_over_build_without_it(reference_build):
+    """With the network's predictions the randomized build factors fewer
+    sketch rows and needs fewer sketch rounds than the same build driven by
+    a prediction-free guess (every box starts from the smallest sketch)."""
+    from skelfmm_gb300.rank_model import LearnedRankPredictor, RankMLP
+
+    class NoModel:
+        def __call__(self, fmm, lev, boxes, x_lev, off):
+            return np.full(boxes.shape[0], 8, dtype=np.int64)
+
+    _, fl, _ = _cube_build(LearnedRankPredictor(RankMLP.load()))
+    _, fn, _ = _cube_build(NoModel())
+    rounds_l = sum(s["sketch_rounds"] for s in fl.level_stats.values())
+    rounds_n = sum(s["sketch_rounds"] for s in fn.level_stats.values())
+    rows_l = sum(s["sketch_rows"] for s in fl.level_stats.values())
+    rows_n = sum(s["sketch_rows"] for s in fn.level_stats.values())
+    assert rounds_l < 0.7 * rounds_n
+    assert rows_l < rows_n
