@@ -403,6 +403,158 @@ __device__ int pivoted_qr(double* A, int m, int n, double tol, int kfix, const Q
   return rank;
 }
 
+// Column-pivoted Householder QR of a small real matrix held in shared memory
+// (s x n, leading dimension ld, n <= blockDim.x): thread j owns column j, so
+// the trailing update needs no cross-lane reduction per column (the FP64
+// pipe, not latency, bounds these factorizations).  Same pivoting, stopping
+// rule, squared-norm downdate and outputs as pivoted_qr (tol rule only).
+__device__ int pivoted_qr_smem(double* Y, int ld, int s, int n, double tol, const QrScratch& q) {
+  __shared__ int s_p;
+  __shared__ double s_h[4];
+  double* vn1 = q.vn1;
+  double* vn2 = q.vn2;
+  double* vv = q.vv;
+  double* red = q.red;
+  int* piv = q.piv;
+  const int j = threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (j < n) {
+    const double* col = Y + (int64_t)j * ld;
+    double a0 = 0, a1 = 0;
+    int i = 0;
+    for (; i + 1 < s; i += 2) {
+      a0 = fma(col[i], col[i], a0);
+      a1 = fma(col[i + 1], col[i + 1], a1);
+    }
+    if (i < s) a0 = fma(col[i], col[i], a0);
+    vn1[j] = a0 + a1;
+    vn2[j] = a0 + a1;
+    piv[j] = j;
+  }
+  __syncthreads();
+  const int kmax = min(s, n);
+  const double tol3z = sqrt(2.220446049250313e-16);
+  double r00 = 0.0;
+  int rank = 0;
+  for (int k = 0; k < kmax; ++k) {
+    // pivot: first index of the largest squared partial norm
+    double best = -1.0;
+    int bi = n;
+    if (j >= k && j < n) {
+      best = vn1[j];
+      bi = j;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      red[warp] = best;
+      reinterpret_cast<int*>(red + 32)[warp] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bb = red[0];
+      int bj = reinterpret_cast<int*>(red + 32)[0];
+      for (int w = 1; w < nw; ++w) {
+        const double ob = red[w];
+        const int oi = reinterpret_cast<int*>(red + 32)[w];
+        if (ob > bb || (ob == bb && oi < bj)) {
+          bb = ob;
+          bj = oi;
+        }
+      }
+      s_p = bj;
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != k) {
+      for (int i = threadIdx.x; i < s; i += blockDim.x) {
+        const double t = Y[(int64_t)k * ld + i];
+        Y[(int64_t)k * ld + i] = Y[(int64_t)p * ld + i];
+        Y[(int64_t)p * ld + i] = t;
+      }
+      if (threadIdx.x == 0) {
+        const int t = piv[k];
+        piv[k] = piv[p];
+        piv[p] = t;
+        const double t1 = vn1[k], t2 = vn2[k];
+        vn1[k] = vn1[p];
+        vn2[k] = vn2[p];
+        vn1[p] = t1;
+        vn2[p] = t2;
+      }
+    }
+    __syncthreads();
+    // Householder reflector of column k (real zlarfg form)
+    const double* ck = Y + (int64_t)k * ld;
+    double sq = 0;
+    for (int i = k + 1 + threadIdx.x; i < s; i += blockDim.x) sq = fma(ck[i], ck[i], sq);
+    const double xnorm2 = block_sum(sq, red);
+    if (threadIdx.x == 0) {
+      const double ar = ck[k];
+      double beta = ar, tau = 0, scl = 0;
+      if (xnorm2 != 0.0) {
+        const double nrm = sqrt(ar * ar + xnorm2);
+        beta = ar >= 0 ? -nrm : nrm;
+        tau = (beta - ar) / beta;
+        scl = 1.0 / (ar - beta);
+      }
+      s_h[0] = beta;
+      s_h[1] = tau;
+      s_h[2] = scl;
+    }
+    __syncthreads();
+    const double beta = s_h[0], tau = s_h[1], scl = s_h[2];
+    if (k == 0) r00 = fabs(beta);
+    if (!(fabs(beta) > tol * r00) || r00 == 0.0) {
+      rank = k;
+      break;
+    }
+    rank = k + 1;
+    for (int i = k + threadIdx.x; i < s; i += blockDim.x) vv[i] = (i == k) ? 1.0 : ck[i] * scl;
+    __syncthreads();
+    if (threadIdx.x == 0) Y[(int64_t)k * ld + k] = beta;
+    // trailing update of the thread's own column
+    if (j > k && j < n) {
+      double* cj = Y + (int64_t)j * ld;
+      double w0 = 0, w1 = 0;
+      int i = k;
+      for (; i + 1 < s; i += 2) {
+        w0 = fma(vv[i], cj[i], w0);
+        w1 = fma(vv[i + 1], cj[i + 1], w1);
+      }
+      if (i < s) w0 = fma(vv[i], cj[i], w0);
+      const double f = tau * (w0 + w1);
+      for (i = k; i < s; ++i) cj[i] = fma(-f, vv[i], cj[i]);
+      const double akj2 = cj[k] * cj[k];
+      const double v1 = vn1[j];
+      const double rem = v1 - akj2;
+      if (v1 != 0.0) {
+        if (rem <= tol3z * vn2[j]) {
+          double p0 = 0, p1 = 0;
+          for (i = k + 1; i + 1 < s; i += 2) {
+            p0 = fma(cj[i], cj[i], p0);
+            p1 = fma(cj[i + 1], cj[i + 1], p1);
+          }
+          if (i < s) p0 = fma(cj[i], cj[i], p0);
+          vn1[j] = p0 + p1;
+          vn2[j] = p0 + p1;
+        } else {
+          vn1[j] = rem;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  return rank;
+}
+
 // T = R11^{-1} R12 (row-major rank x (n - rank)) from the R that pivoted_qr
 // left in A: column back substitution, one warp per right-hand side.
 template <int OP>
@@ -460,8 +612,8 @@ __device__ void write_T(double* A, int m, int n, int rank, double* T, double* ri
   __syncthreads();
 }
 
-template <int OP>
-__global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
+template <int OP, int NT>
+__global__ void __launch_bounds__(NT) k_skel_box(SkelArgs a) {
   constexpr bool C = OpTraits<OP>::kComplex;
   constexpr int D = OpTraits<OP>::kDim;
   constexpr int W = C ? 2 : 1;  // scalars per matrix entry
@@ -511,8 +663,10 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
     int rounds = 0;
     for (int round = 0; 2 * s <= m; ++round, s *= 2) {
       rounds = round + 1;
-      // the sketch lives in shared memory when it fits (latency-bound QR)
-      Y = ((int64_t)s * n * W <= a.ycap) ? sY : gY;
+      // a real sketch that fits in shared memory is factored there, one
+      // thread per column
+      const bool in_smem = !C && n <= (int)blockDim.x && (int64_t)s * n <= a.ycap;
+      Y = in_smem ? sY : gY;
       const uint64_t key = mix64(a.seed ^ ((uint64_t)b << 20) ^ ((uint64_t)round << 52));
       for (int64_t idx = threadIdx.x; idx < (int64_t)s * n; idx += blockDim.x) {
         const int j = (int)(idx / s), t = (int)(idx % s);
@@ -520,7 +674,7 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
         const double* col = A + (int64_t)j * m * W;
         for (int u = 0; u < a.rho; ++u) {
           const uint64_t h = mix64(key + (uint64_t)t * 0x100000001B3ull + (uint64_t)u);
-          const int i = (int)((h >> 1) % (uint64_t)m);
+          const int i = (int)__umulhi((unsigned)(h >> 32), (unsigned)m);  // uniform in [0, m), no division
           const double sg = (h & 1) ? -1.0 : 1.0;
           yr += sg * col[(int64_t)i * W];
           if (C) yi += sg * col[(int64_t)i * W + 1];
@@ -529,7 +683,7 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
         if (C) Y[((int64_t)j * s + t) * W + 1] = yi;
       }
       __syncthreads();
-      rank = pivoted_qr<OP>(Y, s, n, a.sketch_tol, 0, q);
+      rank = in_smem ? pivoted_qr_smem(Y, s, s, n, a.sketch_tol, q) : pivoted_qr<OP>(Y, s, n, a.sketch_tol, 0, q);
       if (rank < n && rank > s - guard) continue;  // saturated: the sketch hides rank
       ok = true;
       break;
@@ -541,7 +695,7 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
       const int nr = n - rank;
       double e2 = 0.0, z2 = 0.0;
       for (int qi = 0; qi < a.nchk; ++qi) {
-        const int row = (int)((mix64(key ^ (0xC0FFEEull + (uint64_t)qi)) >> 1) % (uint64_t)m);
+        const int row = (int)__umulhi((unsigned)(mix64(key ^ (0xC0FFEEull + (uint64_t)qi)) >> 32), (unsigned)m);
         for (int jr = threadIdx.x; jr < n; jr += blockDim.x) {
           const int pj = q.piv[jr];
           const double zr = A[((int64_t)pj * m + row) * W], zi = C ? A[((int64_t)pj * m + row) * W + 1] : 0.0;
@@ -582,16 +736,35 @@ __global__ void __launch_bounds__(kSkelThreads) k_skel_box(SkelArgs a) {
   for (int j = threadIdx.x; j < n; j += blockDim.x) a.perm[off + j] = q.piv[j];
 }
 
+template <int OP, int NT>
+static int launch_skel_nt(const SkelArgs& a, int nbox, size_t smem, cudaStream_t st) {
+  if (smem > 48 * 1024)
+    SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_skel_box<OP, NT><<<nbox, NT, smem, st>>>(a);
+  SKF_CUDA_TRY(cudaGetLastError());
+  return SKF_OK;
+}
+
+// One batch of boxes.  With nbig > 0 the first nbig boxes of a.order (the
+// most expensive) run as 1024-thread blocks on `side`, concurrently with the
+// rest as 256-thread blocks on `st`; `st` then waits for `side`.
 template <int OP>
-static int launch_skel(SkelArgs a, int nbox, int maxn, int maxm, cudaStream_t st) {
+static int launch_skel(SkelArgs a, int nbox, int maxn, int maxm, cudaStream_t st, int nbig = 0,
+                       cudaStream_t side = nullptr, cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
   constexpr int W = OpTraits<OP>::kComplex ? 2 : 1;
   const size_t smem =
       sizeof(double) * ((size_t)2 * maxn + (size_t)maxm * W + 64 + (size_t)a.ycap) + sizeof(int) * (size_t)maxn;
   if (smem > 200 * 1024) return SKF_ERR_UNSUPPORTED;
-  if (smem > 48 * 1024) SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_skel_box<OP><<<nbox, kSkelThreads, smem, st>>>(a);
-  SKF_CUDA_TRY(cudaGetLastError());
-  return SKF_OK;
+  if (nbig <= 0 || nbig >= nbox || !side || !a.order) return launch_skel_nt<OP, kSkelThreads>(a, nbox, smem, st);
+  SKF_CUDA_TRY(cudaEventRecord(e0, st));
+  SKF_CUDA_TRY(cudaStreamWaitEvent(side, e0, 0));
+  int status = launch_skel_nt<OP, 1024>(a, nbig, smem, side);
+  SkelArgs rest = a;
+  rest.order = a.order + nbig;
+  if (status == SKF_OK) status = launch_skel_nt<OP, kSkelThreads>(rest, nbox - nbig, smem, st);
+  SKF_CUDA_TRY(cudaEventRecord(e1, side));
+  SKF_CUDA_TRY(cudaStreamWaitEvent(st, e1, 0));
+  return status;
 }
 
 int proxy_rows(int op, int nproxy) {
@@ -648,6 +821,8 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
   // workspace in batches of boxes bounded by ~4 GiB
   const int64_t budget = (int64_t)4 << 30;
   int status = SKF_OK;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int b0 = 0;
   while (b0 < nbox && status == SKF_OK) {
     std::vector<int64_t> wso;
@@ -673,6 +848,19 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
       ord[b - b0] = b - b0;
     }
     std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
+    // boxes far above an even share of the batch's work get a 1024-thread block
+    double total = 0.0;
+    for (double c : cost) total += c;
+    const double share = total / (152.0 * 4.0);
+    int nbig = 0;
+    while (nbig < (int)ord.size() && cost[ord[nbig]] > 4.0 * share && hoff[b0 + ord[nbig] + 1] - hoff[b0 + ord[nbig]] >= 192)
+      ++nbig;
+    if (nbig > 0 && !side) {
+      if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming) != cudaSuccess)
+        nbig = 0;
+    }
     double* ws = nullptr;
     int64_t* dwso = nullptr;
     int32_t* dord = nullptr;
@@ -729,13 +917,13 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
       if (ra.kpred && hk[b] > 0 && 2 * ((int64_t)hk[b] + ra.oversample) <= mrows && hk[b] < n)
         ymax = std::max<int64_t>(ymax, ((int64_t)hk[b] + ra.oversample) * n * W);
     }
-    // first sketches in shared memory while they are small enough (<= 16 KB)
-    // to keep four blocks per SM
-    a.ycap = ymax <= 2048 ? ymax : 0;
+    // real first sketches up to 64 KB are factored in shared memory (three
+    // blocks per SM)
+    a.ycap = W == 1 ? std::min<int64_t>(ymax, 8192) : 0;
     if (status == SKF_OK) {
       switch (op) {
 #define SKF_CASE(OPID) \
-  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, mrows, st); break;
+  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, mrows, st, nbig, side, ev0, ev1); break;
         SKF_CASE(SKF_LAPLACE_2D)
         SKF_CASE(SKF_LAPLACE_3D)
         SKF_CASE(SKF_HELMHOLTZ_2D)
@@ -754,6 +942,11 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     b0 = b1;
   }
   cudaFreeAsync(dtmpl, st);
+  if (side) {
+    cudaStreamDestroy(side);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+  }
   if (status == SKF_OK) SKF_CUDA_TRY(cudaGetLastError());
   return status;
 }
