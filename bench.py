@@ -5,6 +5,7 @@ skeletonization FMM, 3D Laplace, N = 1,000,000 points uniform in [0,1]^3
 plus the build time and the plain-FP64 apply beside the mixed one.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME]
 
 A step is one apply of the built operator to one charge vector.  ``value`` is
 device-resident throughput (inputs in HBM, CUDA events on the launch stream);
@@ -14,6 +15,15 @@ Multi-GPU runs are independent replicas (one instance per rank, no
 collective on the data path); ``value`` sums all ranks.
 ``--impl reference`` times the reference algorithm's CPU implementation (the
 oracle port of skelfmm's batched apply) on the host cores.
+
+Other workloads (``--workload``): ``laplace2d_square_100k`` (2D Laplace,
+N = 1e5 uniform in [0,1]^2, tol 1e-5, leaf 200), ``helmholtz3d_sphere_2M``
+(3D Helmholtz kappa = 25, N = 2e6 on the unit sphere, complex charges, tol
+1e-6, leaf 400), ``batch64_annulus`` (64 independent 2D Laplace curvy-annulus
+instances, N log-uniform in [1e3, 2e5], tol 1e-6, leaf 128, one captured CUDA
+graph; aggregate Mpts/s) and ``clusters_4M_learned`` (build seconds of the
+learned-rank build against the pivoted-QR build, 3D Laplace, N = 4e6 in 32
+Gaussian clusters, tol 1e-6, leaf 256).
 """
 
 from __future__ import annotations
@@ -32,7 +42,22 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-WORKLOAD = "laplace_3d uniform cube N=1e6 tol=1e-6 leaf=400"
+# name -> (operator, oracle name, point set, N, tol, leaf, kappa, complex charges)
+SINGLE = {
+    "laplace3d_cube_1M": ("LAPLACE_3D", "laplace_3d", "cube", 1_000_000, 1e-6, 400, 0.0, False),
+    "laplace2d_square_100k": ("LAPLACE_2D", "laplace_2d", "square", 100_000, 1e-5, 200, 0.0, False),
+    "helmholtz3d_sphere_2M": ("HELMHOLTZ_3D", "helmholtz_3d", "sphere_surface", 2_000_000, 1e-6, 400, 25.0, True),
+}
+METRIC = {
+    "laplace3d_cube_1M": "apply Mpts/s, 3D Laplace N=1M tol 1e-6 (mixed FP32-kernel apply; plain FP64 apply and "
+                         "build s alongside)",
+    "laplace2d_square_100k": "apply Mpts/s, 2D Laplace N=1e5 tol 1e-5 (mixed apply; FP64 apply and build s alongside)",
+    "helmholtz3d_sphere_2M": "apply Mpts/s, 3D Helmholtz kappa=25 N=2M sphere tol 1e-6 (mixed apply; FP64 apply and "
+                             "build s alongside)",
+    "batch64_annulus": "aggregate apply Mpts/s, 64 independent 2D Laplace curvy-annulus instances, one CUDA graph",
+    "clusters_4M_learned": "build s, 3D Laplace N=4M in 32 Gaussian clusters tol 1e-6: learned-rank build "
+                           "(pivoted-QR build alongside)",
+}
 
 
 def parse():
@@ -41,18 +66,38 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--n", type=int, default=1_000_000)
-    p.add_argument("--tol", type=float, default=1e-6)
-    p.add_argument("--leaf", type=int, default=400)
+    p.add_argument("--workload", default="laplace3d_cube_1M", choices=sorted(METRIC))
+    p.add_argument("--n", type=int, default=None)
+    p.add_argument("--tol", type=float, default=None)
+    p.add_argument("--leaf", type=int, default=None)
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--ncheck", type=int, default=2000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
 
-def workload(n, seed=0):
-    pts = np.random.default_rng(seed).random((n, 3))
+def single_config(args):
+    op, opname, geo, n, tol, leaf, kappa, cplx = SINGLE[args.workload]
+    n = args.n or n
+    tol = args.tol or tol
+    leaf = args.leaf or leaf
+    desc = f"{opname} {geo} N={n:.0e} tol={tol:g} leaf={leaf}" + (f" kappa={kappa:g}" if kappa else "")
+    return dict(op=op, opname=opname, geo=geo, n=n, tol=tol, leaf=leaf, kappa=kappa, cplx=cplx, desc=desc)
+
+
+def workload(cfg, seed=0):
+    rng = np.random.default_rng(seed)
+    n = cfg["n"]
+    if cfg["geo"] == "cube":
+        pts = rng.random((n, 3))
+    elif cfg["geo"] == "square":
+        pts = rng.random((n, 2))
+    else:
+        g = rng.standard_normal((n, 3))
+        pts = g / np.linalg.norm(g, axis=1, keepdims=True)
     x = np.random.RandomState(1).randn(n)
+    if cfg["cplx"]:
+        x = x + 1j * np.random.RandomState(2).randn(n)
     return pts, x
 
 
@@ -133,13 +178,12 @@ def dist_setup():
     return None, 0, 1
 
 
-def cpu_baseline_sample(f, x, budget_s=15.0):
+def cpu_baseline_sample(rb, x, opname="laplace_3d", kappa=0.0, budget_s=15.0):
     """Reference algorithm (oracle port: FP64 dense kernel blocks) on the host
-    cores, over a sample of target boxes of the same build; throughput scaled
-    by pair evaluations (plus the measured upward/downward passes)."""
+    cores, over a sample of target boxes of the same ragged build; throughput
+    scaled by pair evaluations."""
     from oracle import skel_oracle as O
 
-    rb = f.plan.rb
     nb = rb.nboxes
     rng = np.random.default_rng(0)
     order = rng.permutation(nb)
@@ -147,7 +191,7 @@ def cpu_baseline_sample(f, x, budget_s=15.0):
                      sum(rb.box_off[s + 1] - rb.box_off[s] for s in rb.list_src[rb.list_off[b]:rb.list_off[b + 1]])
                      for b in range(nb)], dtype=np.float64)
     total = float(work.sum())
-    q = np.zeros(rb.nentries)
+    q = np.zeros(rb.nentries, dtype=np.asarray(x).dtype)
     q[rb.perm_entry] = x[rb.perm_point]
     qh = q.copy()
     nthreads = os.cpu_count() or 1
@@ -156,7 +200,7 @@ def cpu_baseline_sample(f, x, budget_s=15.0):
         chunk = [b for b in order[i:i + 4 * nthreads] if work[b] > 0]
         i += 4 * nthreads
         t0 = time.perf_counter()
-        res = O.translation_sample("laplace_3d", 0.0, rb.entry_xyz, None, rb.box_off, rb.box_rank,
+        res = O.translation_sample(opname, kappa, rb.entry_xyz, None, rb.box_off, rb.box_rank,
                                    rb.list_off, rb.list_src, rb.list_kind, q, qh, chunk, nthreads)
         secs += time.perf_counter() - t0
         done_pairs += sum(r[2] for r in res)
@@ -168,17 +212,61 @@ def cpu_baseline_sample(f, x, budget_s=15.0):
                       f"evaluation count"}
 
 
-def run_ours(args):
+# FP32 FMA-pipe ops per kernel evaluation in the algorithm: D subtractions and
+# D FMA-pipe ops for r^2, the kernel's own FMA-pipe work, one multiply-add per
+# direction it feeds (complex: 4).  The XU pipe (rsqrt, lg2, sin, cos: 32
+# lanes/clk/SM by ncu pct_of_peak of sm__inst_executed_pipe_xu) does not bind.
+def ops_per_eval(opname, sym):
+    if opname == "laplace_3d":
+        return 8 if sym else 7
+    if opname == "laplace_2d":
+        return 6 if sym else 5
+    if opname == "helmholtz_3d":
+        # + r = r2 * ir, phase, one-turn reduction (2), 2 scalings, complex MAC
+        return 3 + 3 + 1 + 1 + 2 + 2 + 4
+    return None
+
+
+def roofline_line(plan, t_ms, opname, traffic_name):
+    peaks, src = measured_peaks()
+    info = plan.info
+    pairs = int(info.npairs_fused)
+    evals = int(info.npairs_evaluated_mixed)
+    sym = evals < pairs
+    ops = ops_per_eval(opname, sym)
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    kern = (f"k_translate_sym<{opname.upper()}> + k_sym_reduce" if sym else
+            (f"k_translate_f32x2<{opname.upper()}>" if opname.startswith("laplace") else
+             f"k_translate_f32<{opname.upper()}>"))
+    achieved = evals / (t_ms * 1e-3) / 1e9
+    peak = 152 * (128.0 / ops) * sm_mhz * 1e6 / 1e9
+    return {
+        "bound": "fp32-fma", "kernel": kern, "achieved": round(achieved, 1), "peak": round(peak, 1),
+        "unit": "Geval/s", "frac": round(achieved / peak, 4), "traffic": profiled_traffic(traffic_name),
+        "peak_source": f"152 SMs x 128/{ops} evaluations/clk (FP32 FMA pipe, {ops} ops per evaluation) x "
+                       f"sm_max_mhz {sm_mhz:.0f} ({src} MEASURED_PEAKS.json clock); XU pipe not binding",
+        "evaluations_per_launch": evals, "pairs_per_launch": pairs, "launch_ms": round(t_ms, 4),
+        "pairs_per_s_G": round(pairs / (t_ms * 1e-3) / 1e9, 1),
+    }
+
+
+TRAFFIC_PROFILE = {"laplace3d_cube_1M": "translate_sym_lap3d_1M.md"}
+
+
+def run_single(args):
     import torch
 
     from skelfmm_gb300 import _lib, operators
     from skelfmm_gb300.skel_fmm import SkelFMM
 
+    cfg = single_config(args)
+    op = getattr(operators, cfg["op"])
     dist, rank, ws = dist_setup()
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
-    pts, x = workload(args.n, seed=rank)
-    n = args.n
+    pts, x = workload(cfg, seed=rank)
+    n = cfg["n"]
+    W = 2 if cfg["cplx"] else 1
 
     def barrier():
         if dist is not None:
@@ -186,10 +274,10 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
 
     # first use of the library/CUDA context outside the timed build
-    SkelFMM(pts[:2000], operators.LAPLACE_3D, tol=args.tol, leaf_size=args.leaf, precision="mixed")
+    SkelFMM(pts[:20000], op, tol=cfg["tol"], leaf_size=cfg["leaf"], param=cfg["kappa"], precision="mixed")
     barrier()
     t0 = time.perf_counter()
-    f = SkelFMM(pts, operators.LAPLACE_3D, tol=args.tol, leaf_size=args.leaf, precision="mixed")
+    f = SkelFMM(pts, op, tol=cfg["tol"], leaf_size=cfg["leaf"], param=cfg["kappa"], precision="mixed")
     torch.cuda.synchronize(dev)
     build_s = time.perf_counter() - t0
     plan = f.plan
@@ -255,52 +343,27 @@ def run_ours(args):
     err_mixed = float(np.abs(ymix[idx] - yd).max() / den)
     err_fp64 = None if y64 is None else float(np.abs(y64[idx] - yd).max() / den)
 
-    # roofline of the dominant stage (translations, mixed).  Units are kernel
-    # evaluations counted from the built lists.  Per evaluation the algorithm
-    # needs 3 FP32 subtractions, 3 FMA-pipe ops for r^2, 1 rsqrt (XU pipe) and
-    # one FMA per direction it feeds: 7 FMA-pipe ops on the per-direction
-    # path, 8 on the symmetric path (one evaluation feeds both directions).
-    # GB300: 128 FMA-pipe lanes/clk/SM; the XU pipe (32 lanes/clk/SM by ncu
-    # pct_of_peak of sm__inst_executed_pipe_xu) is not binding.
-    # peak = 152 SMs x 128/ops evaluations/clk x max SM clock.  The timed
-    # launch covers the whole translation stage (on the symmetric path the
-    # evaluation kernel plus the partial-sum reduction).
-    peaks, src = measured_peaks()
+    # roofline of the dominant stage (translations, mixed), its device time
     t_ms = plan.time_translations(_lib.PREC_MIXED, reps=5, stream=sp)
-    info = plan.info
-    pairs = int(info.npairs_fused)
-    evals = int(info.npairs_evaluated_mixed)
-    sym = evals < pairs
-    ops = 8 if sym else 7
-    achieved = evals / (t_ms * 1e-3) / 1e9
-    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    peak = 152 * (128.0 / ops) * sm_mhz * 1e6 / 1e9
-    kern = "k_translate_sym<LAPLACE_3D> + k_sym_reduce" if sym else "k_translate_f32x2<LAPLACE_3D>"
-    roofline = {
-        "bound": "fp32-fma", "kernel": kern, "achieved": round(achieved, 1),
-        "peak": round(peak, 1), "unit": "Geval/s", "frac": round(achieved / peak, 4),
-        "traffic": profiled_traffic("translate_sym_lap3d_1M.md" if sym else "translate_lap3d_1M.md"),
-        "peak_source": f"152 SMs x 128/{ops} evaluations/clk (FP32 FMA pipe, {ops} ops per evaluation) x "
-                       f"sm_max_mhz {sm_mhz:.0f} ({src} MEASURED_PEAKS.json clock); XU (rsqrt) not binding",
-        "evaluations_per_launch": evals, "pairs_per_launch": pairs, "launch_ms": round(t_ms, 4),
-        "pairs_per_s_G": round(pairs / (t_ms * 1e-3) / 1e9, 1),
-    }
+    roofline = roofline_line(plan, t_ms, cfg["opname"], TRAFFIC_PROFILE.get(args.workload, ""))
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(f, x)
+        cpu = cpu_baseline_sample(plan.rb, x, cfg["opname"], cfg["kappa"])
     value = n * ws / (ms_step * 1e-3) / 1e6
     line = {
-        "metric": "apply Mpts/s, 3D Laplace N=1M tol 1e-6 (mixed FP32-kernel apply; plain FP64 apply and build s alongside)",
+        "metric": METRIC[args.workload],
         "value": round(value, 2), "unit": "Mpts/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 kernel eval, f64 accumulation", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "N": n, "tol": args.tol, "leaf_size": args.leaf,
-                   "charges": "RandomState(1).randn", "points": "default_rng(rank).random((N,3))",
-                   "l2": "256 MB buffer zeroed between timed steps (outside the step events); working set ~1 GB",
+        "dtype": "f32 kernel eval, f64 accumulation" + (", complex" if cfg["cplx"] else ""), "data": "synthetic",
+        "config": {"workload": cfg["desc"], "N": n, "tol": cfg["tol"], "leaf_size": cfg["leaf"],
+                   "kappa": cfg["kappa"], "points": f"{cfg['geo']}, numpy default_rng(rank)",
+                   "charges": "RandomState(1).randn" + (" + 1j RandomState(2).randn" if cfg["cplx"] else ""),
+                   "l2": "256 MB buffer zeroed between timed steps (outside the step events)",
                    "parallelism": f"replicas x{ws}"},
-        "e2e": {"value": round(n * ws / e2e_s / 1e6, 2), "unit": "Mpts/s", "h2d_bytes_per_step": n * 8,
-                "d2h_bytes_per_step": n * 8, "ms_per_step": round(e2e_s * 1e3, 3)},
-        "gpu_launches": int(info.launches_mixed) * args.steps,
+        "e2e": {"value": round(n * ws / e2e_s / 1e6, 2), "unit": "Mpts/s", "h2d_bytes_per_step": n * 8 * W,
+                "d2h_bytes_per_step": n * 8 * W, "ms_per_step": round(e2e_s * 1e3, 3)},
+        "gpu_launches": int(plan.info.launches_mixed) * args.steps,
+        "gpu_launches_per_step": int(plan.info.launches_mixed),
         "build_s": round(build_s, 3),
         "fp64_ms_per_step": None if ms_fp64 is None else round(ms_fp64, 3),
         "mixed_over_fp64": None if ms_fp64 is None else round(ms_fp64 / ms_step, 2),
@@ -315,85 +378,275 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_reference(args):
-    """The reference algorithm on the host cores (oracle port), bounded sample per step."""
-    import multiprocessing as mp
+def batch_instances(seed=0, ninst=64):
+    """The 64 curvy-annulus instances: N log-uniform in [1e3, 2e5]."""
+    from skelfmm_gb300.tree import get_point_dist
 
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    from oracle import skel_oracle as O
-    from skelfmm_gb300.tree import BalancedTree
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(2e5), ninst)).astype(np.int64)
+    pts = [get_point_dist(n, "curvy_annulus", rng=rng) for n in sizes]
+    xs = [np.random.RandomState(i + 1).randn(n) for i, n in enumerate(sizes)]
+    return pts, xs
 
-    pts, x = workload(args.n)
-    n = args.n
-    ctx = mp.get_context("spawn")
-    ncores = os.cpu_count() or 1
+
+def run_batch(args):
+    import torch
+
+    from skelfmm_gb300 import _lib, operators
+    from skelfmm_gb300.batch import SkelFMMBatch
+    from skelfmm_gb300.tree import get_point_dist
+
+    dist, rank, ws = dist_setup()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    pts, xs = batch_instances(seed=rank)
+    ntot = int(sum(p.shape[0] for p in pts))
+    SkelFMMBatch([get_point_dist(5000, "curvy_annulus", rng=np.random.default_rng(9))], operators.LAPLACE_2D,
+                 tune=False)
+    torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    tree = BalancedTree(pts, args.leaf)
-    # one BLAS thread per pool worker (the workers read these at import; a
-    # multi-threaded BLAS in every worker oversubscribes the cores)
-    blas_env = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
-    saved = {k: os.environ.get(k) for k in blas_env}
-    os.environ.update({k: "1" for k in blas_env})
-    try:
-        pool = ctx.Pool(ncores)
-    finally:
-        for k, v in saved.items():
-            if v is None:
-                os.environ.pop(k, None)
-            else:
-                os.environ[k] = v
-    with pool:
-        ob = O.OracleBuild(tree, O.OPERATORS["laplace_3d"], 0.0, args.tol).skel_tree(500, pool=pool)
+    b = SkelFMMBatch(pts, operators.LAPLACE_2D, tol=1e-6, leaf_size=128, precision="mixed", tune=True)
+    b.capture()
+    torch.cuda.synchronize(dev)
     build_s = time.perf_counter() - t0
-    oa = O.OracleApply(ob, nthreads=ncores)
-    # ragged view of the oracle build for sampled translations
+    b._x.copy_(torch.from_numpy(np.concatenate(xs)))
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        b._graph.replay()
+    torch.cuda.synchronize(dev)
+    evs = []
+    with ClockSampler(dev.index) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b._graph.replay()
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize(dev)
+    ms_step = float(np.mean([a.elapsed_time(c) for a, c in evs]))
+    # e2e: pinned host charges in, graph replay, potentials out
+    xh = torch.from_numpy(np.concatenate(xs)).pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b._x.copy_(xh, non_blocking=True)
+        b._graph.replay()
+        yh.copy_(b._y, non_blocking=True)
+        torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    ys = b.apply(xs)
+    errs = b.relerr(xs, ys, ncheck=200)
+    xs32 = [v.astype(np.float32) for v in xs]
+    errs32 = b.relerr([v.astype(np.float64) for v in xs32], b.apply(xs32), ncheck=200)
+    t_ms = b.plan.time_translations(_lib.PREC_MIXED, reps=5)
+    roofline = roofline_line(b.plan, t_ms, "laplace_2d", "")
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(b.plan.rb, np.concatenate(xs), "laplace_2d", 0.0)
+    value = ntot * ws / (ms_step * 1e-3) / 1e6
+    line = {
+        "metric": METRIC["batch64_annulus"], "value": round(value, 2), "unit": "Mpts/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 kernel eval, f64 accumulation", "data": "synthetic",
+        "config": {"workload": "64 x laplace_2d curvy annulus, N log-uniform [1e3, 2e5] (default_rng(rank)), "
+                               "tol=1e-6 leaf=128", "N_total": ntot, "instances": len(pts),
+                   "tuned_scheme": {"symmetric": int(b.plan.tuned[0]), "packed_shape": int(b.plan.tuned[1])},
+                   "l2": "256 MB buffer zeroed between timed steps (outside the step events)",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": round(ntot * ws / e2e_s / 1e6, 2), "unit": "Mpts/s", "h2d_bytes_per_step": ntot * 8,
+                "d2h_bytes_per_step": ntot * 8, "ms_per_step": round(e2e_s * 1e3, 3)},
+        "gpu_launches": int(b.plan.info.launches_mixed) * args.steps,
+        "gpu_launches_per_step": int(b.plan.info.launches_mixed),
+        "build_s": round(build_s, 3), "tuning_ms": {f"sym{k[0]}_shape{k[1]}": round(v, 3) for k, v in b.tuning.items()},
+        "err_max_f64_charges": float(errs.max()), "err_median_f64_charges": float(np.median(errs)),
+        "err_max_f32_charges": float(errs32.max()), "ncheck_per_instance": 200,
+        "roofline": roofline, "clocks": clk.summary(), "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_clusters(args):
+    import torch
+
+    from skelfmm_gb300 import _lib, operators
+    from skelfmm_gb300.skel_fmm import SkelFMM
+    from skelfmm_gb300.tree import get_point_dist
+
+    dist, rank, ws = dist_setup()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    n = args.n or 4_000_000
+    pts = get_point_dist(n, "gaussian_clusters", rng=np.random.default_rng(rank))
+    x = np.random.RandomState(1).randn(n)
+    for learned in (False, True):  # warm-up builds (module loading, first allocations)
+        SkelFMM(pts[:80000], operators.LAPLACE_3D, tol=1e-6, leaf_size=256, learned_rank=learned).build()
+    torch.cuda.synchronize(dev)
+    idx = np.random.default_rng(0).choice(n, size=min(args.ncheck, n), replace=False)
+    out, yd = {}, None
+    with ClockSampler(dev.index) as clk:
+        for learned in (False, True):
+            t0 = time.perf_counter()
+            f = SkelFMM(pts, operators.LAPLACE_3D, tol=1e-6, leaf_size=256, use_single_precision=True,
+                        learned_rank=learned, keep_host_fmm=True).build()
+            torch.cuda.synchronize(dev)
+            bt = time.perf_counter() - t0
+            if yd is None:
+                yd = f.direct_apply(x, idx)
+            xt = torch.from_numpy(x).to(dev)
+            yt = torch.empty_like(xt)
+            errs = {}
+            for name, prec in (("mixed", _lib.PREC_MIXED), ("fp64", _lib.PREC_FP64)):
+                f.plan.apply_device(xt, yt, prec)
+                torch.cuda.synchronize(dev)
+                y = yt.cpu().numpy()
+                errs[name] = float(np.abs(y[idx] - yd).max() / np.abs(yd).max())
+            st = f.fmm.level_stats
+            out[learned] = {
+                "build_s": round(bt, 3), "tree_s": round(f.tree_time_seconds, 3),
+                "skel_s": round(f.skel_time_seconds, 3), "setup_s": round(f.setup_time_seconds, 3),
+                "err_mixed": errs["mixed"], "err_fp64": errs["fp64"], "rank_max": int(f.rank_max),
+                "randomized_boxes": int(sum(v.get("randomized", 0) for v in st.values())),
+                "randomized_kept": int(sum(v.get("kept", 0) for v in st.values())),
+            }
+            del f
+            torch.cuda.empty_cache()
+    lrn, full = out[True], out[False]
+    line = {
+        "metric": METRIC["clusters_4M_learned"], "value": lrn["build_s"], "unit": "s", "n_gpus": ws, "steps": 1,
+        "warmup": 2, "ms_per_step": round(lrn["build_s"] * 1e3, 1), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (IDs), bf16 (rank network)", "data": "synthetic",
+        "config": {"workload": "laplace_3d 32 Gaussian clusters N=4e6 tol=1e-6 leaf=256", "N": n,
+                   "points": "gaussian_clusters, numpy default_rng(rank)", "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": lrn["build_s"], "unit": "s", "h2d_bytes_per_step": n * 24, "d2h_bytes_per_step": 0},
+        "learned": lrn, "pivoted_qr": full, "speedup_build": round(full["build_s"] / lrn["build_s"], 3),
+        "roofline": None, "clocks": clk.summary(), "cpu_baseline": None,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def oracle_ragged(ob, tree):
+    """Ragged view (entry coordinates, offsets, per-target lists) of an oracle
+    build, for sampled CPU translations."""
     nb = ob.nboxes
     bs = ob.bs_list
     off = np.zeros(nb + 1, dtype=np.int64)
     np.cumsum(bs, out=off[1:])
     xyz = np.concatenate([tree.XX[ob.pid[b]] for b in range(nb) if bs[b] > 0])
     work = {}
-    for u, s in np.vstack((ob.leaf_uskel_from_qskel_list, ob.tree_uskel_from_qskel_list)):
-        work.setdefault(int(u), []).append((int(s), 0))
-    for u, s in ob.uskel_from_q_list:
-        work.setdefault(int(u), []).append((int(s), 1))
-    for u, s in ob.u_from_qskel_list:
-        work.setdefault(int(u), []).append((int(s), 2))
-    for u, s in ob.u_from_q_list:
-        work.setdefault(int(u), []).append((int(s), 3))
+    for u, s_ in np.vstack((ob.leaf_uskel_from_qskel_list, ob.tree_uskel_from_qskel_list)):
+        work.setdefault(int(u), []).append((int(s_), 0))
+    for u, s_ in ob.uskel_from_q_list:
+        work.setdefault(int(u), []).append((int(s_), 1))
+    for u, s_ in ob.u_from_qskel_list:
+        work.setdefault(int(u), []).append((int(s_), 2))
+    for u, s_ in ob.u_from_q_list:
+        work.setdefault(int(u), []).append((int(s_), 3))
     lo = np.zeros(nb + 1, dtype=np.int64)
     srcs, kinds = [], []
     for b in range(nb):
         lst = work.get(b, [])
         lo[b + 1] = lo[b] + len(lst)
-        srcs += [s for s, _ in lst]
+        srcs += [s_ for s_, _ in lst]
         kinds += [k for _, k in lst]
     srcs = np.array(srcs, dtype=np.int64)
     kinds = np.array(kinds, dtype=np.int64)
-    wcost = np.array([bs[b] * sum(bs[s] for s in srcs[lo[b]:lo[b + 1]]) for b in range(nb)], dtype=np.float64)
-    total = float(wcost.sum())
+    wcost = np.array([bs[b] * sum(bs[s_] for s_ in srcs[lo[b]:lo[b + 1]]) for b in range(nb)], dtype=np.float64)
+    return xyz, off, lo, srcs, kinds, wcost
+
+
+def oracle_pool(ncores):
+    """Spawn pool with one BLAS thread per worker (the workers read these at
+    import; a multi-threaded BLAS in every worker oversubscribes the cores)."""
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    blas_env = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in blas_env}
+    os.environ.update({k: "1" for k in blas_env})
+    try:
+        return ctx.Pool(ncores)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def run_reference(args):
+    """The reference algorithm on the host cores (oracle port), bounded sample per step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    if args.workload == "clusters_4M_learned":
+        print(json.dumps({"impl": "reference", "metric": METRIC[args.workload], "unavailable":
+                          "the reference has no learned-rank build; its pivoted-QR CPU build of 4e6 points "
+                          "takes tens of minutes, the pivoted-QR GPU build is this workload's baseline"}),
+              flush=True)
+        return
+    from oracle import skel_oracle as O
+    from skelfmm_gb300.tree import BalancedTree
+
+    ncores = os.cpu_count() or 1
     t0 = time.perf_counter()
-    qv, qhv = oa.upward(x)
-    t_up = time.perf_counter() - t0
-    q = np.concatenate([qv[b] for b in range(nb) if bs[b] > 0])
-    qh = np.concatenate([qhv[b] for b in range(nb) if bs[b] > 0])
+    if args.workload == "batch64_annulus":
+        pts_l, xs = batch_instances()
+        opname, kappa, tol, leaf = "laplace_2d", 0.0, 1e-6, 128
+        desc = "64 x laplace_2d curvy annulus, N log-uniform [1e3, 2e5], tol=1e-6 leaf=128"
+    else:
+        cfg = single_config(args)
+        p_, x_ = workload(cfg)
+        pts_l, xs = [p_], [x_]
+        opname, kappa, tol, leaf = cfg["opname"], cfg["kappa"], cfg["tol"], cfg["leaf"]
+        desc = cfg["desc"]
+    insts = []
+    with oracle_pool(ncores) as pool:
+        for pts, x in zip(pts_l, xs):
+            tree = BalancedTree(pts, leaf)
+            ob = O.OracleBuild(tree, O.OPERATORS[opname], kappa, tol).skel_tree(500, pool=pool)
+            insts.append((tree, ob, x))
+    build_s = time.perf_counter() - t0
+    data, t_up, total, n = [], 0.0, 0.0, 0
+    for tree, ob, x in insts:
+        xyz, off, lo, srcs, kinds, wcost = oracle_ragged(ob, tree)
+        oa = O.OracleApply(ob, nthreads=ncores)
+        t1 = time.perf_counter()
+        qv, qhv = oa.upward(x)
+        t_up += time.perf_counter() - t1
+        bs = ob.bs_list
+        q = np.concatenate([qv[b] for b in range(ob.nboxes) if bs[b] > 0])
+        qh = np.concatenate([qhv[b] for b in range(ob.nboxes) if bs[b] > 0])
+        data.append((xyz, off, ob.rank_list, lo, srcs, kinds, q, qh, wcost))
+        total += float(wcost.sum())
+        n += tree.N
     rng = np.random.default_rng(0)
     per_step = max(1e8, total / 200.0)
+    weights = np.array([d[-1].sum() for d in data])
+    weights = weights / weights.sum()
 
     def step():
-        sel, acc = [], 0.0
-        while acc < per_step:
-            b = int(rng.integers(nb))
-            if wcost[b] > 0:
-                sel.append(b)
-                acc += wcost[b]
-        t = time.perf_counter()
-        res = O.translation_sample("laplace_3d", 0.0, xyz, None, off, ob.rank_list, lo, srcs, kinds, q, qh,
-                                   sel, ncores)
-        dt = time.perf_counter() - t
-        return sum(r[2] for r in res), dt
+        done, secs = 0, 0.0
+        while done < per_step:
+            i = int(rng.choice(len(data), p=weights))
+            xyz, off, rk, lo, srcs, kinds, q, qh, wcost = data[i]
+            nbx = wcost.shape[0]
+            sel, acc = [], 0.0
+            while acc < per_step / 4:
+                b = int(rng.integers(nbx))
+                if wcost[b] > 0:
+                    sel.append(b)
+                    acc += wcost[b]
+            t = time.perf_counter()
+            res = O.translation_sample(opname, kappa, xyz, None, off, rk, lo, srcs, kinds, q, qh, sel, ncores)
+            secs += time.perf_counter() - t
+            done += sum(r[2] for r in res)
+        return done, secs
 
     for _ in range(args.warmup):
         step()
@@ -406,11 +659,10 @@ def run_reference(args):
     t_apply = total / rate + 2 * t_up
     value = n / t_apply / 1e6
     line = {
-        "metric": "apply Mpts/s, 3D Laplace N=1M tol 1e-6 (mixed FP32-kernel apply; plain FP64 apply and build s alongside)",
-        "impl": "reference", "value": round(value, 4), "unit": "Mpts/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_apply * 1e3, 1),
+        "metric": METRIC[args.workload], "impl": "reference", "value": round(value, 4), "unit": "Mpts/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_apply * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "N": n, "tol": args.tol, "leaf_size": args.leaf},
+        "config": {"workload": desc, "N": n, "tol": tol, "leaf_size": leaf},
         "build_s": round(build_s, 2),
         "cpu_baseline": {"value": round(value, 4), "unit": "Mpts/s", "cores": ncores, "kind": "port",
                          "sample": f"{args.steps} steps x ~{per_step:.3g} kernel evaluations of random target "
@@ -425,8 +677,12 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch64_annulus":
+        run_batch(args)
+    elif args.workload == "clusters_4M_learned":
+        run_clusters(args)
     else:
-        run_ours(args)
+        run_single(args)
 
 
 if __name__ == "__main__":
