@@ -141,6 +141,158 @@ __global__ void __launch_bounds__(256) k_up(const int32_t* __restrict__ boxes, c
   }
 }
 
+// ---- float-float variants for the mixed apply ------------------------------
+// GB300's FP64 pipe runs the T / T^T products of the FP64-T kernels above at
+// its peak; here T is held as an FP32 pair (hi = fl32(T), lo = fl32(T - hi))
+// and the vector as a pair likewise, products are formed exactly with FMA
+// (p = a*b, e = fma(a, b, -p)) plus the two cross terms, and sums are
+// carried as (s, c) pairs with Knuth's TwoSum: ~2^-44 relative, all on the
+// FP32 pipes, same 8 bytes of T per scalar.
+struct FF {
+  float s = 0.f, c = 0.f;
+};
+__device__ __forceinline__ void ff_add_prod(FF& acc, float ah, float al, float bh, float bl) {
+  const float p = ah * bh;
+  const float e = fmaf(ah, bh, -p);
+  const float x = fmaf(ah, bl, al * bh);
+  const float t = acc.s + p;
+  const float z = t - acc.s;
+  const float err = (acc.s - (t - z)) + (p - z);
+  acc.s = t;
+  acc.c += err + e + x;
+}
+__device__ __forceinline__ void ff_sub_prod(FF& acc, float ah, float al, float bh, float bl) {
+  ff_add_prod(acc, -ah, -al, bh, bl);
+}
+__device__ __forceinline__ void split_f64(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
+template <bool C>
+__global__ void __launch_bounds__(256) k_up_ff(const int32_t* __restrict__ boxes, const int64_t* __restrict__ box_off,
+                                               const int32_t* __restrict__ box_rank, const int64_t* __restrict__ t_off,
+                                               const float* __restrict__ thi, const float* __restrict__ tlo,
+                                               const int64_t* __restrict__ pslot, double* __restrict__ q,
+                                               double* __restrict__ qh) {
+  extern __shared__ float sm_upf[];  // [2 * nred * W]: hi, lo
+  const int b = boxes[blockIdx.x];
+  const int64_t off = box_off[b];
+  const int bs = (int)(box_off[b + 1] - off);
+  const int r = box_rank[b];
+  const int nred = bs - r;
+  const int W = C ? 2 : 1;
+  float* xh = sm_upf;
+  float* xl = sm_upf + nred * W;
+  for (int c = threadIdx.x; c < nred * W; c += blockDim.x) split_f64(q[(off + r) * W + c], xh[c], xl[c]);
+  __syncthreads();
+  const float* Th = thi + t_off[b] * W;
+  const float* Tl = tlo + t_off[b] * W;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = warp; i < r; i += nw) {
+    const int64_t rb = (int64_t)i * nred * W;
+    FF ar, ai;
+    for (int c = lane; c < nred; c += 32) {
+      if (C) {
+        const float trh = Th[rb + 2 * c], tih = Th[rb + 2 * c + 1];
+        const float trl = Tl[rb + 2 * c], til = Tl[rb + 2 * c + 1];
+        const float xrh = xh[2 * c], xih = xh[2 * c + 1], xrl = xl[2 * c], xil = xl[2 * c + 1];
+        ff_add_prod(ar, trh, trl, xrh, xrl);
+        ff_sub_prod(ar, tih, til, xih, xil);
+        ff_add_prod(ai, trh, trl, xih, xil);
+        ff_add_prod(ai, tih, til, xrh, xrl);
+      } else {
+        ff_add_prod(ar, Th[rb + c], Tl[rb + c], xh[c], xl[c]);
+      }
+    }
+    const double sr = warp_sum((double)ar.s + (double)ar.c);
+    const double si = C ? warp_sum((double)ai.s + (double)ai.c) : 0.0;
+    if (lane == 0) {
+      const int64_t e = off + i;
+      const int64_t ps = pslot[e];
+      if (C) {
+        const double vr = q[2 * e] + sr, vi = q[2 * e + 1] + si;
+        qh[2 * e] = vr;
+        qh[2 * e + 1] = vi;
+        if (ps >= 0) {
+          q[2 * ps] = vr;
+          q[2 * ps + 1] = vi;
+        }
+      } else {
+        const double v = q[e] + sr;
+        qh[e] = v;
+        if (ps >= 0) q[ps] = v;
+      }
+    }
+  }
+}
+
+template <bool C>
+__global__ void __launch_bounds__(256) k_down_ff(const int32_t* __restrict__ boxes,
+                                                 const int64_t* __restrict__ box_off,
+                                                 const int32_t* __restrict__ box_rank,
+                                                 const int64_t* __restrict__ t_off, const float* __restrict__ thi,
+                                                 const float* __restrict__ tlo, const int64_t* __restrict__ pslot,
+                                                 double* __restrict__ u, double* __restrict__ uh) {
+  extern __shared__ float sm_dnf[];  // [2 * r * W]: hi, lo
+  const int b = boxes[blockIdx.x];
+  const int64_t off = box_off[b];
+  const int bs = (int)(box_off[b + 1] - off);
+  const int r = box_rank[b];
+  const int nred = bs - r;
+  const int W = C ? 2 : 1;
+  float* hh = sm_dnf;
+  float* hl = sm_dnf + r * W;
+  for (int i = threadIdx.x; i < r; i += blockDim.x) {
+    const int64_t e = off + i;
+    const int64_t ps = pslot[e];
+    if (C) {
+      double hr = uh[2 * e], hi = uh[2 * e + 1];
+      if (ps >= 0) {
+        hr += u[2 * ps];
+        hi += u[2 * ps + 1];
+      }
+      uh[2 * e] = hr;
+      uh[2 * e + 1] = hi;
+      u[2 * e] += hr;
+      u[2 * e + 1] += hi;
+      split_f64(hr, hh[2 * i], hl[2 * i]);
+      split_f64(hi, hh[2 * i + 1], hl[2 * i + 1]);
+    } else {
+      double h = uh[e];
+      if (ps >= 0) h += u[ps];
+      uh[e] = h;
+      u[e] += h;
+      split_f64(h, hh[i], hl[i]);
+    }
+  }
+  __syncthreads();
+  const float* Th = thi + t_off[b] * W;
+  const float* Tl = tlo + t_off[b] * W;
+  for (int c = threadIdx.x; c < nred; c += blockDim.x) {
+    FF ar, ai;
+    for (int i = 0; i < r; ++i) {
+      const int64_t k = ((int64_t)i * nred + c) * W;
+      if (C) {
+        const float trh = Th[k], tih = Th[k + 1], trl = Tl[k], til = Tl[k + 1];
+        ff_add_prod(ar, trh, trl, hh[2 * i], hl[2 * i]);
+        ff_sub_prod(ar, tih, til, hh[2 * i + 1], hl[2 * i + 1]);
+        ff_add_prod(ai, trh, trl, hh[2 * i + 1], hl[2 * i + 1]);
+        ff_add_prod(ai, tih, til, hh[2 * i], hl[2 * i]);
+      } else {
+        ff_add_prod(ar, Th[k], Tl[k], hh[i], hl[i]);
+      }
+    }
+    const int64_t e = off + r + c;
+    if (C) {
+      u[2 * e] += (double)ar.s + (double)ar.c;
+      u[2 * e + 1] += (double)ai.s + (double)ai.c;
+    } else {
+      u[e] += (double)ar.s + (double)ar.c;
+    }
+  }
+}
+
 // One block per box: uskel[:r] += u(parent slots); u[:r] += uskel[:r];
 // u[r:bs] += T^T uskel[:r].
 template <bool C, typename TT>
@@ -338,6 +490,22 @@ int copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_off, 
   return SKF_OK;
 }
 
+__global__ void k_f64_split(const double* __restrict__ src, float* __restrict__ hi, float* __restrict__ lo, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float h = (float)src[i];
+    hi[i] = h;
+    lo[i] = (float)(src[i] - (double)h);
+  }
+}
+
+int split_f64(const double* src, float* hi, float* lo, int64_t n, cudaStream_t st) {
+  if (n <= 0) return SKF_OK;
+  k_f64_split<<<grid_for(n, 256), 256, 0, st>>>(src, hi, lo, n);
+  SKF_CUDA_TRY(cudaGetLastError());
+  SKF_CUDA_TRY(cudaStreamSynchronize(st));
+  return SKF_OK;
+}
+
 int convert_f64_f32(const double* src, float* dst, int64_t n, cudaStream_t st) {
   if (n <= 0) return SKF_OK;
   k_f64_to_f32<<<grid_for(n, 256), 256, 0, st>>>(src, dst, n);
@@ -352,6 +520,7 @@ int plan_apply_device(skf_plan* p, const double* x, double* y, int precision, cu
   const int W = p->cplx ? 2 : 1;
   const bool mixed = precision != SKF_PREC_FP64;
   const bool t32 = precision == SKF_PREC_MIXED_T32;
+  const bool ff = precision == SKF_PREC_MIXED;  // float-float T / T^T
   SKF_CUDA_TRY(cudaMemsetAsync(p->u, 0, sizeof(double) * p->E * W, st));
   SKF_CUDA_TRY(cudaMemsetAsync(p->uh, 0, sizeof(double) * p->E * W, st));
   const int g = grid_for(p->nperm, 256);
@@ -362,7 +531,10 @@ int plan_apply_device(skf_plan* p, const double* x, double* y, int precision, cu
     const LevelBoxes& L = p->levels[lev];
     if (L.n == 0) continue;
     const size_t sm = sizeof(double) * (size_t)std::max(L.max_red, 1) * W;
-    if (p->cplx) {
+    if (ff) {
+      if (p->cplx) k_up_ff<true><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->t32lo, p->pslot, p->q, p->qh);
+      else k_up_ff<false><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->t32lo, p->pslot, p->q, p->qh);
+    } else if (p->cplx) {
       if (t32) k_up<true, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->q, p->qh);
       else k_up<true, double><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t64, p->pslot, p->q, p->qh);
     } else {
@@ -380,7 +552,10 @@ int plan_apply_device(skf_plan* p, const double* x, double* y, int precision, cu
     const LevelBoxes& L = p->levels[lev];
     if (L.n == 0) continue;
     const size_t sm = sizeof(double) * (size_t)std::max(L.max_rank, 1) * W;
-    if (p->cplx) {
+    if (ff) {
+      if (p->cplx) k_down_ff<true><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->t32lo, p->pslot, p->u, p->uh);
+      else k_down_ff<false><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->t32lo, p->pslot, p->u, p->uh);
+    } else if (p->cplx) {
       if (t32) k_down<true, float><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t32, p->pslot, p->u, p->uh);
       else k_down<true, double><<<L.n, 256, sm, st>>>(L.dev, p->box_off, p->box_rank, p->t_off, p->t64, p->pslot, p->u, p->uh);
     } else {

@@ -31,6 +31,7 @@ int skel_boxes_randomized(int op, double kappa, int nbox, const int64_t* off, co
                           void* t_out, cudaStream_t st);
 int proxy_rows(int op, int nproxy);
 int convert_f64_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
+int split_f64(const double* src, float* hi, float* lo, int64_t n, cudaStream_t st);
 int copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_off, const int64_t* len,
                   const void* src, void* dst, int elem_bytes, cudaStream_t st);
 
@@ -204,10 +205,11 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
       return SKF_ERR_CUDA;
     }
   }
-  // FP32 copy of T, converted on the device
+  // FP32 pair copy of T (hi = fl32(T), lo = fl32(T - hi)), split on the device
   SKF_TRY(upload(p, &p->t32, (const float*)nullptr, (size_t)tl * W));
+  SKF_TRY(upload(p, &p->t32lo, (const float*)nullptr, (size_t)tl * W));
   {
-    const int st = convert_f64_f32(p->t64, p->t32, (int64_t)tl * W, nullptr);
+    const int st = split_f64(p->t64, p->t32, p->t32lo, (int64_t)tl * W, nullptr);
     if (st != SKF_OK) {
       free_plan(p);
       return st;

@@ -85,7 +85,8 @@ struct skf_plan {
   // T blocks
   int64_t* t_off = nullptr;
   double* t64 = nullptr;
-  float* t32 = nullptr;
+  float* t32 = nullptr;    // fl32(T)
+  float* t32lo = nullptr;  // fl32(T - fl32(T)): float-float T of the mixed apply
   // interaction lists
   int64_t* list_off = nullptr;
   int32_t* list_src = nullptr;
