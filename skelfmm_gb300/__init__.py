@@ -2,13 +2,16 @@
 
 Public surface mirrors ``skelfmm/__init__.py``: ``SkelFMM``,
 ``RecursiveSkeletonization``, ``operators`` and ``warmup_cuda_fmm_apply``;
-``Plan`` is the device-resident apply (the role of ``SkelFMMBatched``).
+``Plan`` is the device-resident apply (the role of ``SkelFMMBatched``);
+``SkelFMMBatch`` applies many independent instances as one operator and
+``RankMLP`` is the rank network of the learned-rank build.
 """
 
 from . import operators  # noqa: F401
 from .tree import BalancedTree  # noqa: F401
 
-__all__ = ["SkelFMM", "RecursiveSkeletonization", "Plan", "operators", "warmup_cuda_fmm_apply", "BalancedTree"]
+__all__ = ["SkelFMM", "RecursiveSkeletonization", "Plan", "SkelFMMBatch", "RankMLP", "operators",
+           "warmup_cuda_fmm_apply", "BalancedTree"]
 
 
 def __getattr__(name):
@@ -24,4 +27,12 @@ def __getattr__(name):
         from .plan import Plan
 
         return Plan
+    if name == "SkelFMMBatch":
+        from .batch import SkelFMMBatch
+
+        return SkelFMMBatch
+    if name == "RankMLP":
+        from .rank_model import RankMLP
+
+        return RankMLP
     raise AttributeError(f"module {__name__!r} has no attribute {name!r}")
