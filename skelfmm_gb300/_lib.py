@@ -26,6 +26,7 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_MIXED_T32 = 2
 
+OPT_SCALAR_MIXED, OPT_PACKED_SHAPE, OPT_SYMMETRIC, OPT_SYM_SHAPE = 1, 2, 3, 4
 KIND_COLLEAGUE = 0
 KIND_COARSE_UP = 1
 KIND_COARSE_DOWN = 2

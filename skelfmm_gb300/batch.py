@@ -77,26 +77,9 @@ def concat_ragged(rbs):
 
 
 def autotune(plan: Plan, precision=_lib.PREC_MIXED, reps=3):
-    """Time the translation schemes this plan supports and keep the fastest.
-
-    Candidates: symmetric evaluation on/off, and for the per-direction packed
-    kernel its three block shapes.  Returns {setting: ms}.
-    """
-    results = {}
-    best = None
-    for sym in (1, 0):
-        for shape in ((0,) if sym else (0, 1, 2)):
-            plan.set_option(3, sym)
-            plan.set_option(2, shape)
-            plan.time_translations(precision, reps=1)
-            ms = plan.time_translations(precision, reps=reps)
-            results[(sym, shape)] = ms
-            if best is None or ms < results[best]:
-                best = (sym, shape)
-    plan.set_option(3, best[0])
-    plan.set_option(2, best[1])
-    plan.tuned = best
-    return results
+    """Time the translation schemes this plan supports and keep the fastest
+    (``Plan.autotune``).  Returns {setting: ms}."""
+    return plan.autotune(precision, reps)
 
 
 class SkelFMMBatch:

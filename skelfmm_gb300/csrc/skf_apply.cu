@@ -355,6 +355,17 @@ __global__ void __launch_bounds__(256) k_down(const int32_t* __restrict__ boxes,
 }
 
 // ------------------------------------------------------------------ dispatch
+template <int OP, int TS, int MINB>
+static void launch_sym(const SymArgs& c, int n, cudaStream_t st) {
+  constexpr size_t smem = sym_smem_bytes(TS);
+  static bool attr = false;  // per instantiation
+  if (!attr) {
+    cudaFuncSetAttribute(k_translate_sym<OP, TS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  k_translate_sym<OP, TS, MINB><<<n, 128, smem, st>>>(c);
+}
+
 template <int OP>
 static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
   TransArgs a;
@@ -414,7 +425,16 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
           c.pbuf = p->pbuf;
           c.u = p->u;
           c.uh = p->uh;
-          if (p->worksym.n > 0) k_translate_sym<OP><<<p->worksym.n, 128, 0, st>>>(c);
+          if (p->worksym.n > 0) {
+            // tile shape: 0 = 64 sources, 5 blocks/SM; 1 = 128 sources, 3 blocks/SM;
+            // 2 = 64 sources, 4 blocks/SM; 3 = 32 sources, 5 blocks/SM
+            switch (p->sym_shape) {
+              case 1: launch_sym<OP, 128, 3>(c, p->worksym.n, st); break;
+              case 2: launch_sym<OP, 64, 4>(c, p->worksym.n, st); break;
+              case 3: launch_sym<OP, 32, 5>(c, p->worksym.n, st); break;
+              default: launch_sym<OP, 64, 5>(c, p->worksym.n, st); break;
+            }
+          }
           k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
               p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
           return;

@@ -445,6 +445,10 @@ int skf_plan_set_option(skf_plan* p, int32_t option, int64_t value) {
   switch (option) {
     case SKF_OPT_SCALAR_MIXED: p->scalar_mixed = value != 0; return SKF_OK;
     case SKF_OPT_SYMMETRIC: p->sym_on = value != 0; return SKF_OK;
+    case SKF_OPT_SYM_SHAPE:
+      if (value < 0 || value > 3) return SKF_ERR_ARG;
+      p->sym_shape = (int)value;
+      return SKF_OK;
     case SKF_OPT_PACKED_SHAPE:
       if (value < 0 || value > 2) return SKF_ERR_ARG;
       p->x2_config = (int)value;

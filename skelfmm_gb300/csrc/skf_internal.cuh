@@ -51,6 +51,7 @@ struct skf_plan {
   bool cplx = false;
   bool scalar_mixed = false;  // force the scalar FP32 translation kernel (comparison/testing)
   int x2_config = 0;          // packed kernel: 0 = 4 warps x 1 pair, 1 = 1 x 4, 2 = 2 x 2
+  int sym_shape = 0;          // symmetric kernel tile shape (SKF_OPT_SYM_SHAPE)
   // symmetric translations (mixed path, symmetric point kernels, symmetric lists)
   bool sym_ok = false;  // usable for this plan
   bool sym_on = true;   // option SKF_OPT_SYMMETRIC

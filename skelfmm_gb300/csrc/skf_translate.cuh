@@ -609,13 +609,18 @@ struct SymArgs {
 };
 
 constexpr int kSymPairs = 2;  // packed row pairs per lane (4 rows)
-constexpr int kSymTS = 64;    // sources per shared-memory tile
-constexpr int kSymLd = kSymTS + 2;  // row stride = 2 (mod 32): lanes (lr, ls) write distinct banks
+// Sources per shared-memory tile (TS, a multiple of 32) and the row stride of
+// the B-side partial tile, TS + 2 = 2 (mod 32): the lanes (lr, ls) of a warp
+// write 32 distinct banks.
+__host__ __device__ constexpr int sym_ld(int ts) { return ts + 2; }
+__host__ __device__ constexpr size_t sym_smem_bytes(int ts) {
+  return 4 * sizeof(ulonglong2) * (size_t)ts + 2 * 4 * 16 * sizeof(float) * (size_t)sym_ld(ts);
+}
 
 // One tile: lane (lr, ls) evaluates its 4 rows against sources j = 2g + ls.
 // Row sums accumulate in registers; the lane's B-side sum for source j (its 4
 // rows) goes to sTu[lr][j] / sTh[lr][j] and is reduced after the tile.
-template <int D, bool HR, bool HT, bool TR, bool SELF, bool LOG>
+template <int D, bool HR, bool HT, bool TR, bool SELF, bool LOG, int LD>
 __device__ __forceinline__ void sym_tile(const ulonglong2* __restrict__ s0, const ulonglong2* __restrict__ s1,
                                          const ulonglong2* __restrict__ s2, const ulonglong2* __restrict__ s3,
                                          int nt, int ls, int lr, const f2_t (&thx)[kSymPairs],
@@ -623,8 +628,8 @@ __device__ __forceinline__ void sym_tile(const ulonglong2* __restrict__ s0, cons
                                          const f2_t (&tlx)[kSymPairs], const f2_t (&tly)[kSymPairs],
                                          const f2_t (&tlz)[kSymPairs], const f2_t (&c1T)[kSymPairs],
                                          const f2_t (&c2T)[kSymPairs], f2_t (&pu)[kSymPairs],
-                                         f2_t (&ph)[kSymPairs], float (*__restrict__ sTu)[kSymLd],
-                                         float (*__restrict__ sTh)[kSymLd]) {
+                                         f2_t (&ph)[kSymPairs], float* __restrict__ sTu,
+                                         float* __restrict__ sTh) {
 #pragma unroll 4
   for (int j = ls; j < nt; j += 2) {
     const ulonglong2 A = s0[j];   // (-hx,-hx), (-hy,-hy)
@@ -661,24 +666,28 @@ __device__ __forceinline__ void sym_tile(const ulonglong2* __restrict__ s0, cons
     if (TR) {
       float a, b;
       f2_unpack(tu, a, b);
-      sTu[lr][j] = a + b;
+      sTu[lr * LD + j] = a + b;
       if (HT) {
         f2_unpack(th, a, b);
-        sTh[lr][j] = a + b;
+        sTh[lr * LD + j] = a + b;
       }
     }
   }
 }
 
-template <int OP>
-__global__ void __launch_bounds__(128, 5) k_translate_sym(SymArgs a) {
+template <int OP, int TS, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_translate_sym(SymArgs a) {
   constexpr int D = OpTraits<OP>::kDim;
   constexpr bool LOG = (OP == SKF_LAPLACE_2D);
-  constexpr int TS = kSymTS;
   constexpr int NW = 4;
-  __shared__ ulonglong2 s0[TS], s1[TS], s2[TS], s3[TS];
-  __shared__ float sTu[NW][16][kSymLd];
-  __shared__ float sTh[NW][16][kSymLd];
+  constexpr int LD = sym_ld(TS);
+  extern __shared__ __align__(16) unsigned char sym_sm[];
+  ulonglong2* s0 = reinterpret_cast<ulonglong2*>(sym_sm);
+  ulonglong2* s1 = s0 + TS;
+  ulonglong2* s2 = s1 + TS;
+  ulonglong2* s3 = s2 + TS;
+  float* sTu = reinterpret_cast<float*>(s3 + TS);  // [NW][16][LD]
+  float* sTh = sTu + NW * 16 * LD;
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int lr = lane & 15, ls = lane >> 4;
@@ -771,18 +780,18 @@ __global__ void __launch_bounds__(128, 5) k_translate_sym(SymArgs a) {
       f2_t pu[kSymPairs], ph[kSymPairs];
 #pragma unroll
       for (int p = 0; p < kSymPairs; ++p) pu[p] = ph[p] = zero;
-      float(*tu)[kSymLd] = sTu[warp];
-      float(*thp)[kSymLd] = sTh[warp];
+      float* tu = sTu + warp * 16 * LD;
+      float* thp = sTh + warp * 16 * LD;
       if (active) {
         if (self) {
-          if (hr) sym_tile<D, true, false, false, true, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
-          else sym_tile<D, false, false, false, true, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          if (hr) sym_tile<D, true, false, false, true, LOG, LD>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          else sym_tile<D, false, false, false, true, LOG, LD>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
         } else if (hr) {
-          if (ht) sym_tile<D, true, true, true, false, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
-          else sym_tile<D, true, false, true, false, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          if (ht) sym_tile<D, true, true, true, false, LOG, LD>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          else sym_tile<D, true, false, true, false, LOG, LD>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
         } else {
-          if (ht) sym_tile<D, false, true, true, false, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
-          else sym_tile<D, false, false, true, false, LOG>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          if (ht) sym_tile<D, false, true, true, false, LOG, LD>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
+          else sym_tile<D, false, false, true, false, LOG, LD>(s0, s1, s2, s3, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, tu, thp);
         }
 #pragma unroll
         for (int p = 0; p < kSymPairs; ++p) {
@@ -796,27 +805,30 @@ __global__ void __launch_bounds__(128, 5) k_translate_sym(SymArgs a) {
           for (int k = lane; k < 16 * TS; k += 32) {
             const int rr = k / TS, jj = k - rr * TS;
             if (jj < nt) {
-              if (!active) tu[rr][jj] = 0.f;
-              thp[rr][jj] = 0.f;
+              if (!active) tu[rr * LD + jj] = 0.f;
+              thp[rr * LD + jj] = 0.f;
             }
           }
         }
         __syncthreads();
-        // threads 0..63 add the u partials of source j = tid, threads 64..127
-        // the uh partials: 4 warps x 16 lanes each, consecutive j per thread
-        const int j = threadIdx.x & (TS - 1);
-        const bool hpart = threadIdx.x >= TS;
-        if (j < nt) {
-          float (*src)[16][kSymLd] = hpart ? sTh : sTu;
-          float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
+        // index i < TS: u partials of source j = i, TS <= i < 2 TS: the uh
+        // partials of source i - TS; 4 warps x 16 lanes each, consecutive j
+        // per thread
+        for (int i = threadIdx.x; i < 2 * TS; i += NW * 32) {
+          const int j = i & (TS - 1);
+          const bool hpart = i >= TS;
+          if (j < nt) {
+            const float* src = hpart ? sTh : sTu;
+            float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
 #pragma unroll
-          for (int r = 0; r < 16; ++r) {
-            v0 += src[0][r][j];
-            v1 += src[1][r][j];
-            v2 += src[2][r][j];
-            v3 += src[3][r][j];
+            for (int r = 0; r < 16; ++r) {
+              v0 += src[(0 * 16 + r) * LD + j];
+              v1 += src[(1 * 16 + r) * LD + j];
+              v2 += src[(2 * 16 + r) * LD + j];
+              v3 += src[(3 * 16 + r) * LD + j];
+            }
+            a.pbuf[pblk + (hpart ? bsS : 0) + t0 + j] = (v0 + v1) + (v2 + v3);
           }
-          a.pbuf[pblk + (hpart ? bsS : 0) + t0 + j] = (v0 + v1) + (v2 + v3);
         }
       }
       t0 += nt;

@@ -235,6 +235,34 @@ class Plan:
     def set_option(self, option, value):
         _lib.check(_lib.load().skf_plan_set_option(self._h, int(option), int(value)), "skf_plan_set_option")
 
+    def autotune(self, precision=_lib.PREC_MIXED, reps=3):
+        """Time the translation schemes this plan supports and keep the
+        fastest: the symmetric kernel's four tile shapes (Laplace plans with
+        symmetric lists) and the per-direction packed kernel's three block
+        shapes.  Returns {(symmetric, shape): ms}; the choice is kept in
+        ``self.tuned``."""
+        self.set_option(_lib.OPT_SYMMETRIC, 1)
+        info = self._query()
+        sym_ok = info.npairs_evaluated_mixed < info.npairs_fused
+        cands = ([(1, sh) for sh in range(4)] if sym_ok else []) + [(0, sh) for sh in range(3)]
+        results = {}
+        for sym, shape in cands:
+            self.set_option(_lib.OPT_SYMMETRIC, sym)
+            self.set_option(_lib.OPT_SYM_SHAPE if sym else _lib.OPT_PACKED_SHAPE, shape)
+            self.time_translations(precision, reps=1)
+            results[(sym, shape)] = self.time_translations(precision, reps=reps)
+        best = min(results, key=results.get)
+        self.set_option(_lib.OPT_SYMMETRIC, best[0])
+        self.set_option(_lib.OPT_SYM_SHAPE if best[0] else _lib.OPT_PACKED_SHAPE, best[1])
+        self.info = self._query()
+        self.tuned = best
+        return results
+
+    def _query(self):
+        info = _lib.PlanInfo()
+        _lib.check(_lib.load().skf_plan_query(self._h, ctypes.byref(info)), "skf_plan_query")
+        return info
+
     def time_translations(self, precision, reps=5, stream=None):
         ms = ctypes.c_float()
         _lib.check(_lib.load().skf_plan_time_translations(self._h, int(precision), int(reps),

@@ -175,6 +175,10 @@ class SkelFMM:
             t0 = perf_counter()
             fmm.setup_lists(verbose=verbose)
             self.plan = Plan(fmm.ragged())
+            self.tuning = None
+            if self._prec_code != _lib.PREC_FP64:
+                # translation scheme and tile shape for this plan, by timing them
+                self.tuning = self.plan.autotune(self._prec_code, reps=2)
             torch.cuda.synchronize(self.device)
             self.setup_time_seconds = perf_counter() - t0
         self.build_time_seconds = perf_counter() - t_build
