@@ -15,6 +15,7 @@
 //   3. T = R11^{-1} R12 by column-oriented back substitution (util.py:41-49).
 // The proxy matrix lives column-major in a global workspace (L2-resident for
 // leaf-sized boxes); one warp owns a column during each trailing update.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -736,6 +737,275 @@ __global__ void __launch_bounds__(NT) k_skel_box(SkelArgs a) {
   for (int j = threadIdx.x; j < n; j += blockDim.x) a.perm[off + j] = q.piv[j];
 }
 
+// ---- one box on a thread-block cluster -------------------------------------
+// The costliest boxes of a level (candidate sets of ~1,000-1,500 points) set
+// the level's time when one block factors each.  Here a cluster of
+// kClusterCTAs blocks, each on its own SM, factors one box: block r owns the
+// physical columns j = r (mod kClusterCTAs) of the column-major proxy matrix
+// in global memory.  Per elimination step: every block publishes its best
+// candidate (squared partial norm, position) in shared memory; after a
+// cluster barrier every block reads all candidates through distributed
+// shared memory and applies the same logical swap of positions k and p; the
+// pivot column's owner builds the Householder vector and publishes it; after
+// a second cluster barrier every block copies it and updates its own
+// columns.  Same pivoting rule (first position of the largest norm), stopping
+// rule, squared-norm downdate and outputs as pivoted_qr + write_T.  Every
+// block runs the same steps and cluster barriers: the stop decision reads the
+// published |R_kk| after a barrier, so it is uniform over the cluster.
+constexpr int kClusterCTAs = 8;
+
+template <int OP>
+__global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThreads)
+    k_skel_box_cluster(SkelArgs a) {
+  static_assert(!OpTraits<OP>::kComplex, "real operators only");
+  namespace cg = cooperative_groups;
+  constexpr int D = OpTraits<OP>::kDim;
+  constexpr int NC = kClusterCTAs;
+  cg::cluster_group cl = cg::this_cluster();
+  const int cr = (int)cl.block_rank();
+  const int lb = a.order[blockIdx.x / NC];
+  const int b = a.first_box + lb;
+  const int64_t off = a.off[b];
+  const int n = (int)(a.off[b + 1] - off);
+  const int m = a.mrows;
+  const int ncl = (n + NC - 1) / NC;
+  double* A = a.ws + a.ws_off[lb];
+  extern __shared__ double smc[];
+  double* vsh = smc;           // [m] Householder vector published by the pivot's owner
+  double* vloc = vsh + m;      // [m] local copy (later: reciprocal diagonal)
+  double* red = vloc + m;      // [64]
+  double* pub = red + 64;      // [4] candidate norm, candidate position, beta, tau
+  double* vn1 = pub + 4;       // [ncl] squared partial norms of the owned columns
+  double* vn2 = vn1 + ncl;     // [ncl]
+  int* piv = reinterpret_cast<int*>(vn2 + ncl);  // [n] position -> physical column
+  int* posof = piv + n;                          // [n] physical column -> position
+  __shared__ int s_col;
+  __shared__ double s_h[3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double c[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
+
+  // ---- proxy matrix, owned columns only
+  for (int64_t idx = threadIdx.x; idx < (int64_t)m * ncl; idx += blockDim.x) {
+    const int jl = (int)(idx / m), i = (int)(idx % m);
+    const int j = cr + NC * jl;
+    if (j >= n) continue;
+    double kr, ki;
+    proxy_entry<OP>(a, c, i, a.x + (off + j) * D, a.geom ? a.geom + (off + j) * 3 : nullptr, kr, ki);
+    A[(int64_t)j * m + i] = kr;
+  }
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    piv[j] = j;
+    posof[j] = j;
+  }
+  __syncthreads();
+  for (int jl = warp; jl < ncl; jl += nw) {
+    const int j = cr + NC * jl;
+    if (j >= n) continue;
+    const double* col = A + (int64_t)j * m;
+    double s = 0;
+    for (int i = lane; i < m; i += 32) s += col[i] * col[i];
+    s = warp_sum_d(s);
+    if (lane == 0) {
+      vn1[jl] = s;
+      vn2[jl] = s;
+    }
+  }
+  __syncthreads();
+
+  const int kmax = min(m, n);
+  const bool fixed = a.tol >= 1.0;
+  const int rank_fixed = fixed ? min((int)a.tol, kmax) : kmax;
+  const double tol3z = sqrt(2.220446049250313e-16);
+  double r00 = 0.0;
+  int rank = 0;
+  for (int k = 0; k < kmax; ++k) {
+    // ---- this block's candidate: largest norm, first position on ties
+    double best = -1.0;
+    int bpos = 0x7fffffff;
+    for (int jl = threadIdx.x; jl < ncl; jl += blockDim.x) {
+      const int j = cr + NC * jl;
+      if (j >= n) continue;
+      const int pos = posof[j];
+      if (pos < k) continue;
+      const double v = vn1[jl];
+      if (v > best || (v == best && pos < bpos)) {
+        best = v;
+        bpos = pos;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int op = __shfl_xor_sync(0xffffffffu, bpos, o);
+      if (ob > best || (ob == best && op < bpos)) {
+        best = ob;
+        bpos = op;
+      }
+    }
+    if (lane == 0) {
+      red[warp] = best;
+      reinterpret_cast<int*>(red + 32)[warp] = bpos;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bb = red[0];
+      int bp = reinterpret_cast<int*>(red + 32)[0];
+      for (int w = 1; w < nw; ++w) {
+        const double ob = red[w];
+        const int op = reinterpret_cast<int*>(red + 32)[w];
+        if (ob > bb || (ob == bb && op < bp)) {
+          bb = ob;
+          bp = op;
+        }
+      }
+      pub[0] = bb;
+      pub[1] = (double)bp;
+    }
+    cl.sync();  // candidates published
+    // ---- the cluster's pivot and the logical swap of positions k and p
+    if (threadIdx.x == 0) {
+      double gb = -1.0;
+      int gp = 0x7fffffff;
+      for (int r = 0; r < NC; ++r) {
+        const double* rp = cl.map_shared_rank(pub, r);
+        const double v = rp[0];
+        const int p = (int)rp[1];
+        if (v > gb || (v == gb && p < gp)) {
+          gb = v;
+          gp = p;
+        }
+      }
+      const int ck = piv[k], cp = piv[gp];
+      piv[k] = cp;
+      piv[gp] = ck;
+      posof[cp] = k;
+      posof[ck] = gp;
+      s_col = cp;
+    }
+    __syncthreads();
+    const int col = s_col;
+    const int owner = col % NC;
+    if (cr == owner) {
+      // Householder reflector of column col, rows k..m-1 (real zlarfg form)
+      double* ckc = A + (int64_t)col * m;
+      double sq = 0;
+      for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) sq += ckc[i] * ckc[i];
+      const double xnorm2 = block_sum(sq, red);
+      if (threadIdx.x == 0) {
+        const double ar = ckc[k];
+        double beta = ar, tau = 0, scl = 0;
+        if (xnorm2 != 0.0) {
+          const double nrm = sqrt(ar * ar + xnorm2);
+          beta = ar >= 0 ? -nrm : nrm;
+          tau = (beta - ar) / beta;
+          scl = 1.0 / (ar - beta);
+        }
+        s_h[0] = beta;
+        s_h[1] = tau;
+        s_h[2] = scl;
+        pub[2] = beta;
+        pub[3] = tau;
+      }
+      __syncthreads();
+      const double scl = s_h[2];
+      for (int i = k + threadIdx.x; i < m; i += blockDim.x) vsh[i] = (i == k) ? 1.0 : ckc[i] * scl;
+      __syncthreads();
+      if (threadIdx.x == 0) ckc[k] = s_h[0];
+    }
+    cl.sync();  // reflector published
+    const double* opub = cl.map_shared_rank(pub, owner);
+    const double beta = opub[2], tau = opub[3];
+    if (k == 0) r00 = fabs(beta);
+    const bool stop = fixed ? (k >= rank_fixed) : (!(fabs(beta) > a.tol * r00) || r00 == 0.0);
+    if (stop) {
+      rank = k;
+      break;
+    }
+    rank = k + 1;
+    const double* ov = cl.map_shared_rank(vsh, owner);
+    for (int i = k + threadIdx.x; i < m; i += blockDim.x) vloc[i] = ov[i];
+    __syncthreads();
+    // ---- trailing update of the owned columns at positions > k
+    for (int jl = warp; jl < ncl; jl += nw) {
+      const int j = cr + NC * jl;
+      if (j >= n || posof[j] <= k) continue;
+      double* cj = A + (int64_t)j * m;
+      double w = 0;
+      for (int i = k + lane; i < m; i += 32) w += vloc[i] * cj[i];
+      w = warp_sum_d(w);
+      const double f = tau * w;
+      double part = 0;
+      for (int i = k + lane; i < m; i += 32) {
+        const double v = cj[i] - vloc[i] * f;
+        cj[i] = v;
+        if (i > k) part += v * v;
+      }
+      __syncwarp();
+      const double akj = cj[k];
+      const double v1 = vn1[jl];
+      const double rem = v1 - akj * akj;
+      const bool recompute = v1 != 0.0 && rem <= tol3z * vn2[jl];
+      if (recompute) {
+        part = warp_sum_d(part);
+        if (lane == 0) {
+          vn1[jl] = part;
+          vn2[jl] = part;
+        }
+      } else if (lane == 0 && v1 != 0.0) {
+        vn1[jl] = rem;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+  cl.sync();  // every update of the proxy matrix is visible; no remote reads follow
+
+  // ---- outputs: rank and permutation (block 0), T of the owned redundant columns
+  if (cr == 0) {
+    if (threadIdx.x == 0) {
+      a.rank[b] = rank;
+      if (a.status) a.status[b] = 0;
+      if (a.resid) a.resid[b] = -1.0;
+    }
+    for (int pos = threadIdx.x; pos < n; pos += blockDim.x) a.perm[off + pos] = piv[pos];
+  }
+  const int nr = n - rank;
+  if (rank == 0 || nr == 0) return;
+  double* rinv = vloc;
+  for (int i = threadIdx.x; i < rank; i += blockDim.x) rinv[i] = 1.0 / A[(int64_t)piv[i] * m + i];
+  __syncthreads();
+  double* T = a.t_out + a.t_off_out[b];
+  for (int jl = warp; jl < ncl; jl += nw) {
+    const int j = cr + NC * jl;
+    if (j >= n) continue;
+    const int pos = posof[j];
+    if (pos < rank) continue;
+    const int cidx = pos - rank;
+    double* bcol = A + (int64_t)j * m;  // R12 column, overwritten by t
+    for (int i = rank - 1; i >= 0; --i) {
+      const double* ci = A + (int64_t)piv[i] * m;
+      const double t = bcol[i] * rinv[i];
+      __syncwarp();
+      if (lane == 0) bcol[i] = t;
+      for (int l = lane; l < i; l += 32) bcol[l] -= ci[l] * t;
+      __syncwarp();
+    }
+    for (int i = lane; i < rank; i += 32) T[(int64_t)i * nr + cidx] = bcol[i];
+  }
+}
+
+template <int OP>
+static int launch_skel_cluster(const SkelArgs& a, int nbox, int maxn, cudaStream_t st) {
+  const int ncl = (maxn + kClusterCTAs - 1) / kClusterCTAs;
+  const size_t smem = sizeof(double) * ((size_t)2 * a.mrows + 64 + 4 + 2 * (size_t)ncl) + sizeof(int) * 2 * (size_t)maxn;
+  if (smem > 200 * 1024) return SKF_ERR_UNSUPPORTED;
+  if (smem > 48 * 1024)
+    SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box_cluster<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_skel_box_cluster<OP><<<nbox * kClusterCTAs, kSkelThreads, smem, st>>>(a);
+  SKF_CUDA_TRY(cudaGetLastError());
+  return SKF_OK;
+}
+
 template <int OP, int NT>
 static int launch_skel_nt(const SkelArgs& a, int nbox, size_t smem, cudaStream_t st) {
   if (smem > 48 * 1024)
@@ -746,8 +1016,10 @@ static int launch_skel_nt(const SkelArgs& a, int nbox, size_t smem, cudaStream_t
 }
 
 // One batch of boxes.  With nbig > 0 the first nbig boxes of a.order (the
-// most expensive) run as 1024-thread blocks on `side`, concurrently with the
-// rest as 256-thread blocks on `st`; `st` then waits for `side`.
+// most expensive) run on `side` — one thread-block cluster per box for real
+// operators (full pivoted-QR ID), one 1024-thread block otherwise —
+// concurrently with the rest as 256-thread blocks on `st`; `st` then waits
+// for `side`.
 template <int OP>
 static int launch_skel(SkelArgs a, int nbox, int maxn, int maxm, cudaStream_t st, int nbig = 0,
                        cudaStream_t side = nullptr, cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
@@ -758,7 +1030,9 @@ static int launch_skel(SkelArgs a, int nbox, int maxn, int maxm, cudaStream_t st
   if (nbig <= 0 || nbig >= nbox || !side || !a.order) return launch_skel_nt<OP, kSkelThreads>(a, nbox, smem, st);
   SKF_CUDA_TRY(cudaEventRecord(e0, st));
   SKF_CUDA_TRY(cudaStreamWaitEvent(side, e0, 0));
-  int status = launch_skel_nt<OP, 1024>(a, nbig, smem, side);
+  int status;
+  if constexpr (!OpTraits<OP>::kComplex) status = launch_skel_cluster<OP>(a, nbig, maxn, side);
+  else status = launch_skel_nt<OP, 1024>(a, nbig, smem, side);
   SkelArgs rest = a;
   rest.order = a.order + nbig;
   if (status == SKF_OK) status = launch_skel_nt<OP, kSkelThreads>(rest, nbox - nbig, smem, st);
@@ -853,7 +1127,9 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     for (double c : cost) total += c;
     const double share = total / (152.0 * 4.0);
     int nbig = 0;
-    while (nbig < (int)ord.size() && cost[ord[nbig]] > 4.0 * share && hoff[b0 + ord[nbig] + 1] - hoff[b0 + ord[nbig]] >= 192)
+    // (real operators: a cluster per box from twice an even share)
+    const double big = (W == 1 ? 2.0 : 4.0) * share;
+    while (nbig < (int)ord.size() && cost[ord[nbig]] > big && hoff[b0 + ord[nbig] + 1] - hoff[b0 + ord[nbig]] >= 192)
       ++nbig;
     if (nbig > 0 && !side) {
       if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
