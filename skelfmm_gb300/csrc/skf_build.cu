@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <random>
 #include <vector>
 
 #include "skf_internal.cuh"
@@ -106,14 +107,14 @@ struct SkelArgs {
   const int64_t* t_off_out;
   double* t_out;
   int first_box;
-  // randomized mode: box b with kpred[b] > 0 first factors sketches
-  // Y = S K of its proxy matrix (S a sparse sign matrix with `rho` nonzeros
-  // per row drawn from `seed`), starting with kpred[b] + oversample rows and
-  // doubling while the rank found on Y (|R_kk| <= sketch_tol |R_00|) comes
-  // within `oversample / 2` of the sketch size; the ID of the first
-  // unsaturated sketch is checked on nchk hashed rows of K and kept when its
-  // relative Frobenius residual is <= resid_tol, else the box runs the full
-  // pivoted-QR ID of K.
+  // randomized mode: box b with kpred[b] > 0 first factors the sketch
+  // Y = S K of its proxy matrix, kpred[b] + oversample rows of the launch's
+  // sparse sign matrix S (`rho` entries +-1 per row, drawn on the host from
+  // `seed`, shared by all boxes: S does not depend on K).  If the rank found
+  // on Y (|R_kk| <= sketch_tol |R_00|) comes within oversample / 2 of the
+  // sketch size the sketch is saturated; otherwise the ID is checked on nchk
+  // hashed rows of K and kept when its relative Frobenius residual is <=
+  // resid_tol.  Saturated or rejected boxes run the full pivoted-QR ID of K.
   const int32_t* kpred;
   int oversample;
   int rho;
@@ -124,6 +125,7 @@ struct SkelArgs {
   double* resid;    // [nbox] residual of the randomized ID (-1: not tried)
   int8_t* status;   // [nbox] 0 full QR; else 10 * sketch rounds + (1 kept, 2 rejected)
   int64_t ycap;     // doubles of dynamic shared memory for the sketch (0: none)
+  const int32_t* sk_tab;  // [sk_rows * rho] sketch entries: proxy row | sign bit 31
   const int32_t* order;  // block -> box of the batch, longest first (NULL: identity)
 };
 
@@ -190,6 +192,43 @@ struct QrScratch {
   double* red;  // [64] reduction scratch
   int* piv;     // [n] column permutation
 };
+
+// One warp applies the real reflector I - tau v v^T to rows k..m-1 of the
+// column cj (m - k <= 32 * kColRegs): the column slice is loaded into
+// registers with every load in flight, so a step costs one round trip to L2
+// per column instead of one per 32 rows.  Returns the squared norm of rows
+// > k after the update in `part` and the updated row-k entry in `akj`.
+constexpr int kColRegs = 24;
+__device__ __forceinline__ void warp_reflect_column(double* __restrict__ cj, const double* __restrict__ vv, int k,
+                                                    int m, double tau, int lane, double& part, double& akj) {
+  double cr[kColRegs];
+#pragma unroll
+  for (int q = 0; q < kColRegs; ++q) {
+    const int i = k + lane + 32 * q;
+    cr[q] = (i < m) ? cj[i] : 0.0;
+  }
+  double w0 = 0, w1 = 0;
+#pragma unroll
+  for (int q = 0; q < kColRegs; q += 2) {
+    const int i = k + lane + 32 * q;
+    if (i < m) w0 = fma(vv[i], cr[q], w0);
+    if (i + 32 < m) w1 = fma(vv[i + 32], cr[q + 1], w1);
+  }
+  const double f = tau * warp_sum_d(w0 + w1);
+  double p = 0;
+#pragma unroll
+  for (int q = 0; q < kColRegs; ++q) {
+    const int i = k + lane + 32 * q;
+    if (i < m) {
+      const double v = fma(-vv[i], f, cr[q]);
+      cr[q] = v;
+      cj[i] = v;
+      if (i > k) p = fma(v, v, p);
+    }
+  }
+  part = p;
+  akj = __shfl_sync(0xffffffffu, cr[0], 0);
+}
 
 // Column-pivoted Householder QR of the m x n column-major matrix A (leading
 // dimension m), stopped at rank kfix (> 0) or at |R_kk| <= tol |R_00|.
@@ -349,6 +388,27 @@ __device__ int pivoted_qr(double* A, int m, int n, double tol, int kfix, const Q
       if (C) ck[k * W + 1] = 0.0;
     }
     // trailing update: A(k:, j) -= conj(tau) v (v^H A(k:, j)), one warp per column
+    if (!C && m - k <= 32 * kColRegs) {
+      for (int j = k + 1 + warp; j < n; j += nw) {
+        double part, akj;
+        warp_reflect_column(A + (int64_t)j * m, vv, k, m, taur, lane, part, akj);
+        const double v1 = vn1[j];
+        const double rem = v1 - akj * akj;
+        const bool recompute = v1 != 0.0 && rem <= tol3z * vn2[j];
+        if (recompute) {
+          part = warp_sum_d(part);
+          if (lane == 0) {
+            vn1[j] = part;
+            vn2[j] = part;
+          }
+        } else if (lane == 0 && v1 != 0.0) {
+          vn1[j] = rem;
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+      continue;
+    }
     for (int j = k + 1 + warp; j < n; j += nw) {
       double* cj = A + (int64_t)j * m * W;
       double wr = 0, wi = 0;
@@ -613,8 +673,10 @@ __device__ void write_T(double* A, int m, int n, int rank, double* T, double* ri
   __syncthreads();
 }
 
-template <int OP, int NT>
-__global__ void __launch_bounds__(NT) k_skel_box(SkelArgs a) {
+// RAND: the launch carries randomized boxes (a.kpred); that variant keeps
+// three blocks per SM for its latency-bound sketch factorizations.
+template <int OP, int NT, bool RAND>
+__global__ void __launch_bounds__(NT, NT <= 256 ? (RAND ? 3 : 2) : 1) k_skel_box(SkelArgs a) {
   constexpr bool C = OpTraits<OP>::kComplex;
   constexpr int D = OpTraits<OP>::kDim;
   constexpr int W = C ? 2 : 1;  // scalars per matrix entry
@@ -624,7 +686,7 @@ __global__ void __launch_bounds__(NT) k_skel_box(SkelArgs a) {
   const int64_t off = a.off[b];
   const int n = (int)(a.off[b + 1] - off);
   const int m = a.mrows;
-  const int kp = a.kpred ? a.kpred[b] : 0;
+  const int kp = (RAND && a.kpred) ? a.kpred[b] : 0;
   // randomized ID while the sketch is well below the proxy matrix
   int s = kp > 0 ? kp + a.oversample : 0;
   const bool sketch = kp > 0 && 2 * s <= m && kp < n;
@@ -661,33 +723,34 @@ __global__ void __launch_bounds__(NT) k_skel_box(SkelArgs a) {
     double* Y = gY;
     const int guard = max(2, a.oversample / 2);
     bool ok = false;
-    int rounds = 0;
-    for (int round = 0; 2 * s <= m; ++round, s *= 2) {
-      rounds = round + 1;
+    const int rounds = 1;
+    {
       // a real sketch that fits in shared memory is factored there, one
       // thread per column
       const bool in_smem = !C && n <= (int)blockDim.x && (int64_t)s * n <= a.ycap;
       Y = in_smem ? sY : gY;
-      const uint64_t key = mix64(a.seed ^ ((uint64_t)b << 20) ^ ((uint64_t)round << 52));
       for (int64_t idx = threadIdx.x; idx < (int64_t)s * n; idx += blockDim.x) {
         const int j = (int)(idx / s), t = (int)(idx % s);
         double yr = 0, yi = 0;
         const double* col = A + (int64_t)j * m * W;
+        const int32_t* row = a.sk_tab + (int64_t)t * a.rho;
         for (int u = 0; u < a.rho; ++u) {
-          const uint64_t h = mix64(key + (uint64_t)t * 0x100000001B3ull + (uint64_t)u);
-          const int i = (int)__umulhi((unsigned)(h >> 32), (unsigned)m);  // uniform in [0, m), no division
-          const double sg = (h & 1) ? -1.0 : 1.0;
-          yr += sg * col[(int64_t)i * W];
-          if (C) yi += sg * col[(int64_t)i * W + 1];
+          const int32_t e = row[u];
+          const int i = e & 0x7fffffff;
+          if (e < 0) {
+            yr -= col[(int64_t)i * W];
+            if (C) yi -= col[(int64_t)i * W + 1];
+          } else {
+            yr += col[(int64_t)i * W];
+            if (C) yi += col[(int64_t)i * W + 1];
+          }
         }
         Y[((int64_t)j * s + t) * W] = yr;
         if (C) Y[((int64_t)j * s + t) * W + 1] = yi;
       }
       __syncthreads();
       rank = in_smem ? pivoted_qr_smem(Y, s, s, n, a.sketch_tol, q) : pivoted_qr<OP>(Y, s, n, a.sketch_tol, 0, q);
-      if (rank < n && rank > s - guard) continue;  // saturated: the sketch hides rank
-      ok = true;
-      break;
+      ok = !(rank < n && rank > s - guard);  // saturated: the sketch hides rank
     }
     if (ok) {
       write_T<OP>(Y, s, n, rank, T, q.vn1);
@@ -720,7 +783,7 @@ __global__ void __launch_bounds__(NT) k_skel_box(SkelArgs a) {
       done = res <= a.resid_tol;
       if (threadIdx.x == 0 && a.resid) a.resid[b] = res;
     } else if (threadIdx.x == 0 && a.resid) {
-      a.resid[b] = -2.0;  // every sketch saturated
+      a.resid[b] = -2.0;  // the sketch saturated
     }
     if (threadIdx.x == 0 && a.status) a.status[b] = (int8_t)(10 * rounds + (done ? 1 : 2));
     __syncthreads();
@@ -930,18 +993,22 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
       const int j = cr + NC * jl;
       if (j >= n || posof[j] <= k) continue;
       double* cj = A + (int64_t)j * m;
-      double w = 0;
-      for (int i = k + lane; i < m; i += 32) w += vloc[i] * cj[i];
-      w = warp_sum_d(w);
-      const double f = tau * w;
-      double part = 0;
-      for (int i = k + lane; i < m; i += 32) {
-        const double v = cj[i] - vloc[i] * f;
-        cj[i] = v;
-        if (i > k) part += v * v;
+      double part = 0, akj;
+      if (m - k <= 32 * kColRegs) {
+        warp_reflect_column(cj, vloc, k, m, tau, lane, part, akj);
+      } else {
+        double w = 0;
+        for (int i = k + lane; i < m; i += 32) w += vloc[i] * cj[i];
+        w = warp_sum_d(w);
+        const double f = tau * w;
+        for (int i = k + lane; i < m; i += 32) {
+          const double v = cj[i] - vloc[i] * f;
+          cj[i] = v;
+          if (i > k) part += v * v;
+        }
+        __syncwarp();
+        akj = cj[k];
       }
-      __syncwarp();
-      const double akj = cj[k];
       const double v1 = vn1[jl];
       const double rem = v1 - akj * akj;
       const bool recompute = v1 != 0.0 && rem <= tol3z * vn2[jl];
@@ -1008,9 +1075,15 @@ static int launch_skel_cluster(const SkelArgs& a, int nbox, int maxn, cudaStream
 
 template <int OP, int NT>
 static int launch_skel_nt(const SkelArgs& a, int nbox, size_t smem, cudaStream_t st) {
-  if (smem > 48 * 1024)
-    SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_skel_box<OP, NT><<<nbox, NT, smem, st>>>(a);
+  if (a.kpred) {
+    if (smem > 48 * 1024)
+      SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_skel_box<OP, NT, true><<<nbox, NT, smem, st>>>(a);
+  } else {
+    if (smem > 48 * 1024)
+      SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_skel_box<OP, NT, false><<<nbox, NT, smem, st>>>(a);
+  }
   SKF_CUDA_TRY(cudaGetLastError());
   return SKF_OK;
 }
@@ -1091,6 +1164,24 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
   double* dtmpl = nullptr;
   SKF_CUDA_TRY(cudaMallocAsync(&dtmpl, sizeof(double) * tmpl.size(), st));
   SKF_CUDA_TRY(cudaMemcpyAsync(dtmpl, tmpl.data(), sizeof(double) * tmpl.size(), cudaMemcpyHostToDevice, st));
+  // sparse sign sketch shared by the launch: sk_rows x rho entries, each a
+  // uniform proxy row with a random sign (bit 31)
+  int32_t* dtab = nullptr;
+  std::vector<int32_t> tab;
+  if (ra.kpred) {
+    int sk_rows = 1;
+    for (int b = 0; b < nbox; ++b)
+      if (hk[b] > 0) sk_rows = std::max<int>(sk_rows, std::min<int>(hk[b] + ra.oversample, mrows / 2));
+    tab.resize((size_t)sk_rows * ra.rho);
+    std::mt19937_64 gen(ra.seed);
+    for (auto& e : tab) {
+      const uint64_t h = gen();
+      const int32_t i = (int32_t)((h >> 1) % (uint64_t)mrows);
+      e = (h & 1) ? (int32_t)((uint32_t)i | 0x80000000u) : i;
+    }
+    SKF_CUDA_TRY(cudaMallocAsync(&dtab, sizeof(int32_t) * tab.size(), st));
+    SKF_CUDA_TRY(cudaMemcpyAsync(dtab, tab.data(), sizeof(int32_t) * tab.size(), cudaMemcpyHostToDevice, st));
+  }
 
   // workspace in batches of boxes bounded by ~4 GiB
   const int64_t budget = (int64_t)4 << 30;
@@ -1177,6 +1268,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     a.t_out = static_cast<double*>(t_out);
     a.first_box = b0;
     a.kpred = ra.kpred;
+    a.sk_tab = dtab;
     a.oversample = ra.oversample;
     a.rho = ra.rho;
     a.seed = ra.seed;
@@ -1193,9 +1285,11 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
       if (ra.kpred && hk[b] > 0 && 2 * ((int64_t)hk[b] + ra.oversample) <= mrows && hk[b] < n)
         ymax = std::max<int64_t>(ymax, ((int64_t)hk[b] + ra.oversample) * n * W);
     }
-    // real first sketches up to 64 KB are factored in shared memory (three
-    // blocks per SM)
-    a.ycap = W == 1 ? std::min<int64_t>(ymax, 8192) : 0;
+    // sketches are factored in global memory by the warp-per-column QR with
+    // register-resident columns (faster than the shared-memory
+    // thread-per-column QR, pivoted_qr_smem, at these sizes)
+    a.ycap = 0;
+    (void)ymax;
     if (status == SKF_OK) {
       switch (op) {
 #define SKF_CASE(OPID) \
@@ -1218,6 +1312,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     b0 = b1;
   }
   cudaFreeAsync(dtmpl, st);
+  if (dtab) cudaFreeAsync(dtab, st);
   if (side) {
     cudaStreamDestroy(side);
     cudaEventDestroy(ev0);

@@ -235,7 +235,7 @@ class LearnedRankPredictor:
     detects its rank with a stricter rule on the sketch, a few above the
     pivoted-QR rank), capped at the box size.  It sets the first sketch size."""
 
-    def __init__(self, model: RankMLP, margin=4):
+    def __init__(self, model: RankMLP, margin=8):
         self.model = model
         self.margin = int(margin)
 
