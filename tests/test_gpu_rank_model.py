@@ -157,8 +157,9 @@ def test_network_gains_over_build_without_it(reference_build):
         def __call__(self, fmm, lev, boxes, x_lev, off):
             return np.full(boxes.shape[0], 8, dtype=np.int64)
 
-    _, fl, _ = _cube_build(LearnedRankPredictor(RankMLP.load()))
-    _, fn, _ = _cube_build(NoModel())
+    # boxes of ~200 points with ranks ~120: sketches are smaller than boxes
+    _, fl, _ = _cube_build(LearnedRankPredictor(RankMLP.load()), n=100000, leaf=256)
+    _, fn, _ = _cube_build(NoModel(), n=100000, leaf=256)
     kept_l = sum(s["kept"] for s in fl.level_stats.values())
     kept_n = sum(s["kept"] for s in fn.level_stats.values())
     fb_l = sum(s["fallback"] for s in fl.level_stats.values())
