@@ -237,7 +237,8 @@ def roofline_line(plan, t_ms, opname, traffic_name):
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
     kern = (f"k_translate_sym<{opname.upper()}> + k_sym_reduce" if sym else
             (f"k_translate_f32x2<{opname.upper()}>" if opname.startswith("laplace") else
-             f"k_translate_f32<{opname.upper()}>"))
+             ("k_translate_helm_x2 (packed FP32x2)" if opname == "helmholtz_3d" else
+              f"k_translate_f32<{opname.upper()}>")))
     achieved = evals / (t_ms * 1e-3) / 1e9
     peak = 152 * (128.0 / ops) * sm_mhz * 1e6 / 1e9
     return {

@@ -449,6 +449,16 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
           return;
         }
       }
+      if constexpr (OP == SKF_HELMHOLTZ_3D) {
+        if (!p->scalar_mixed) {
+          switch (p->x2_config) {
+            case 1: k_translate_helm_x2<1, 4><<<p->work32.n, 32, 0, st>>>(b); break;
+            case 2: k_translate_helm_x2<2, 2><<<p->work32.n, 64, 0, st>>>(b); break;
+            default: k_translate_helm_x2<4, 1><<<p->work32.n, 128, 0, st>>>(b); break;
+          }
+          return;
+        }
+      }
       k_translate_f32<OP><<<p->work32.n, kT32Threads, 0, st>>>(b);
     }
   } else {

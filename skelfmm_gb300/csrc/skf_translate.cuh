@@ -565,6 +565,203 @@ __global__ void __launch_bounds__(NW * 32) k_translate_f32x2(TransArgs32 a) {
   }
 }
 
+// ------------------------------------------------------------------ Helmholtz 3D, packed
+// exp(i kappa r) / r with complex charges, two target rows per FP32x2
+// instruction: differences, r^2, r, the phase in turns, its one-turn
+// remainder, the scalings by 1/r and the four complex multiply-adds are
+// packed; rsqrt, rint, sin and cos stay per lane.  Sources are staged
+// pre-negated and duplicated, with the charges as (c1r, c1i), (-c1i, c2r),
+// (c2i, -c2i).  Same arithmetic per evaluation as k_translate_f32 (hi/lo
+// differences, one-turn phase reduction, compensated FP32 sums).
+template <int NP, bool H, bool SELF>
+__device__ __forceinline__ void hx2_tile(const ulonglong2* __restrict__ s0, const ulonglong2* __restrict__ s1,
+                                         const ulonglong2* __restrict__ s2, const ulonglong2* __restrict__ s3,
+                                         const ulonglong2* __restrict__ s4, const ulonglong2* __restrict__ s5, int nt,
+                                         const f2_t (&thx)[NP], const f2_t (&thy)[NP], const f2_t (&thz)[NP],
+                                         const f2_t (&tlx)[NP], const f2_t (&tly)[NP], const f2_t (&tlz)[NP],
+                                         f2_t kc2, f2_t (&pur)[NP], f2_t (&pui)[NP], f2_t (&phr)[NP],
+                                         f2_t (&phi)[NP]) {
+  const f2_t two_pi = f2_pack(6.283185307179586f, 6.283185307179586f);
+#pragma unroll 2
+  for (int j = 0; j < nt; ++j) {
+    const ulonglong2 A = s0[j];   // (-hx), (-hy)
+    const ulonglong2 B = s1[j];   // (-hz), (-lx)
+    const ulonglong2 Cc = s2[j];  // (-ly), (-lz)
+    const ulonglong2 Q1 = s3[j];  // c1r, c1i
+    const ulonglong2 Q2 = s4[j];  // -c1i, c2r
+    const ulonglong2 Q3 = s5[j];  // c2i, -c2i
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const f2_t dx = f2_add(f2_add(thx[p], A.x), f2_add(tlx[p], B.y));
+      const f2_t dy = f2_add(f2_add(thy[p], A.y), f2_add(tly[p], Cc.x));
+      const f2_t dz = f2_add(f2_add(thz[p], B.x), f2_add(tlz[p], Cc.y));
+      f2_t r2 = f2_mul(dx, dx);
+      r2 = f2_fma(dy, dy, r2);
+      r2 = f2_fma(dz, dz, r2);
+      float ra, rb;
+      f2_unpack(r2, ra, rb);
+      float ia = rsqrt_approx(ra), ib = rsqrt_approx(rb);
+      if (SELF) {
+        ia = ra > 0.f ? ia : 0.f;
+        ib = rb > 0.f ? ib : 0.f;
+      }
+      const f2_t ir = f2_pack(ia, ib);
+      const f2_t t = f2_mul(f2_mul(r2, ir), kc2);  // phase in turns: kappa r / (2 pi)
+      float ta, tb;
+      f2_unpack(t, ta, tb);
+      const f2_t ang = f2_mul(f2_add(t, f2_pack(-rintf(ta), -rintf(tb))), two_pi);
+      float aa, ab;
+      f2_unpack(ang, aa, ab);
+      float sa, ca, sb, cb;
+      asm("sin.approx.ftz.f32 %0, %1;" : "=f"(sa) : "f"(aa));
+      asm("cos.approx.ftz.f32 %0, %1;" : "=f"(ca) : "f"(aa));
+      asm("sin.approx.ftz.f32 %0, %1;" : "=f"(sb) : "f"(ab));
+      asm("cos.approx.ftz.f32 %0, %1;" : "=f"(cb) : "f"(ab));
+      const f2_t kr = f2_mul(f2_pack(ca, cb), ir);
+      const f2_t ki = f2_mul(f2_pack(sa, sb), ir);
+      pur[p] = f2_fma(ki, Q2.x, f2_fma(kr, Q1.x, pur[p]));
+      pui[p] = f2_fma(ki, Q1.x, f2_fma(kr, Q1.y, pui[p]));
+      if (H) {
+        phr[p] = f2_fma(ki, Q3.y, f2_fma(kr, Q2.y, phr[p]));
+        phi[p] = f2_fma(ki, Q2.y, f2_fma(kr, Q3.x, phi[p]));
+      }
+    }
+  }
+}
+
+template <int NW, int NP>
+__global__ void __launch_bounds__(NW * 32) k_translate_helm_x2(TransArgs32 a) {
+  constexpr int TS = kTileSrcF32;
+  static_assert(64 * NW * NP == 256, "work items are 256-row tiles");
+  __shared__ ulonglong2 s0[TS], s1[TS], s2[TS], s3[TS], s4[TS], s5[TS];
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int U = a.work_box[blockIdx.x];
+  const int row0 = a.work_row[blockIdx.x];
+  const int64_t offU = a.box_off[U];
+  const int bsU = (int)(a.box_off[U + 1] - offU);
+  const int rU = a.box_rank[U];
+  const int wrow0 = row0 + 64 * NP * warp;
+  const bool active = wrow0 < bsU;
+  const float kc = a.kappa * 0.15915494309189535f;
+  const f2_t kc2 = f2_pack(kc, kc);
+
+  f2_t thx[NP], thy[NP], thz[NP], tlx[NP], tly[NP], tlz[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const int ra = wrow0 + lane + 64 * p, rb = ra + 32;
+    const int64_t ea = offU + max(0, min(ra, bsU - 1)), eb = offU + max(0, min(rb, bsU - 1));
+    const float4 ha = a.hi32[ea], hb = a.hi32[eb];
+    const float4 la = a.lo32[ea], lb = a.lo32[eb];
+    thx[p] = f2_pack(ha.x, hb.x);
+    thy[p] = f2_pack(ha.y, hb.y);
+    thz[p] = f2_pack(ha.z, hb.z);
+    tlx[p] = f2_pack(la.x, lb.x);
+    tly[p] = f2_pack(la.y, lb.y);
+    tlz[p] = f2_pack(la.z, lb.z);
+  }
+  const bool need_h = wrow0 < rU;
+  const f2_t zero = 0ull;
+  f2_t sur[NP], cur[NP], sui[NP], cui[NP], shr[NP], chr[NP], shi[NP], chi[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) sur[p] = cur[p] = sui[p] = cui[p] = shr[p] = chr[p] = shi[p] = chi[p] = zero;
+
+  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
+  for (int64_t l = l0; l < l1; ++l) {
+    const int s = a.list_src[l];
+    const int kind = a.list_kind[l];
+    const int64_t offS = a.box_off[s];
+    const int bsS = (int)(a.box_off[s + 1] - offS);
+    const int rS = a.box_rank[s];
+    const int nh = (kind == SKF_KIND_COLLEAGUE) ? rS : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
+    const bool self = (s == U);
+    const float* c1src = (kind == SKF_KIND_COARSE_DOWN) ? a.qd32 : a.q32;
+    for (int t0 = 0; t0 < bsS;) {
+      const bool hseg = t0 < nh;
+      const int nt = min(TS, (hseg ? nh : bsS) - t0);
+      __syncthreads();
+      for (int j = threadIdx.x; j < nt; j += NW * 32) {
+        const int64_t e = offS + t0 + j;
+        const float4 h = a.hi32[e], lo = a.lo32[e];
+        const float c1r = c1src[2 * e], c1i = c1src[2 * e + 1];
+        float c2r = 0.f, c2i = 0.f;
+        if (kind == SKF_KIND_COLLEAGUE) {
+          c2r = a.qhn32[2 * e];
+          c2i = a.qhn32[2 * e + 1];
+        } else if (kind == SKF_KIND_COARSE_UP) {
+          c2r = -c1r;
+          c2i = -c1i;
+        }
+        s0[j] = make_ulonglong2(f2_pack(-h.x, -h.x), f2_pack(-h.y, -h.y));
+        s1[j] = make_ulonglong2(f2_pack(-h.z, -h.z), f2_pack(-lo.x, -lo.x));
+        s2[j] = make_ulonglong2(f2_pack(-lo.y, -lo.y), f2_pack(-lo.z, -lo.z));
+        s3[j] = make_ulonglong2(f2_pack(c1r, c1r), f2_pack(c1i, c1i));
+        s4[j] = make_ulonglong2(f2_pack(-c1i, -c1i), f2_pack(c2r, c2r));
+        s5[j] = make_ulonglong2(f2_pack(c2i, c2i), f2_pack(-c2i, -c2i));
+      }
+      __syncthreads();
+      if (active) {
+        f2_t pur[NP], pui[NP], phr[NP], phi[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) pur[p] = pui[p] = phr[p] = phi[p] = zero;
+        const bool doh = need_h && hseg;
+        if (doh) {
+          if (self) hx2_tile<NP, true, true>(s0, s1, s2, s3, s4, s5, nt, thx, thy, thz, tlx, tly, tlz, kc2, pur, pui, phr, phi);
+          else hx2_tile<NP, true, false>(s0, s1, s2, s3, s4, s5, nt, thx, thy, thz, tlx, tly, tlz, kc2, pur, pui, phr, phi);
+        } else {
+          if (self) hx2_tile<NP, false, true>(s0, s1, s2, s3, s4, s5, nt, thx, thy, thz, tlx, tly, tlz, kc2, pur, pui, phr, phi);
+          else hx2_tile<NP, false, false>(s0, s1, s2, s3, s4, s5, nt, thx, thy, thz, tlx, tly, tlz, kc2, pur, pui, phr, phi);
+        }
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          f2_two_sum(sur[p], cur[p], pur[p]);
+          f2_two_sum(sui[p], cui[p], pui[p]);
+          if (doh) {
+            f2_two_sum(shr[p], chr[p], phr[p]);
+            f2_two_sum(shi[p], chi[p], phi[p]);
+          }
+        }
+      }
+      t0 += nt;
+    }
+  }
+  if (!active) return;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    float a0, b0, a1, b1;
+    const int ra = wrow0 + lane + 64 * p, rb = ra + 32;
+    double ur[2], ui[2], hr[2], hi[2];
+    f2_unpack(sur[p], a0, b0);
+    f2_unpack(cur[p], a1, b1);
+    ur[0] = (double)a0 + (double)a1;
+    ur[1] = (double)b0 + (double)b1;
+    f2_unpack(sui[p], a0, b0);
+    f2_unpack(cui[p], a1, b1);
+    ui[0] = (double)a0 + (double)a1;
+    ui[1] = (double)b0 + (double)b1;
+    f2_unpack(shr[p], a0, b0);
+    f2_unpack(chr[p], a1, b1);
+    hr[0] = (double)a0 + (double)a1;
+    hr[1] = (double)b0 + (double)b1;
+    f2_unpack(shi[p], a0, b0);
+    f2_unpack(chi[p], a1, b1);
+    hi[0] = (double)a0 + (double)a1;
+    hi[1] = (double)b0 + (double)b1;
+    const int rows[2] = {ra, rb};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int row = rows[q];
+      if (row >= bsU) continue;
+      const int64_t e = offU + row;
+      const bool sk = row < rU;
+      a.u[2 * e] = ur[q];
+      a.u[2 * e + 1] = ui[q];
+      a.uh[2 * e] = sk ? hr[q] : 0.0;
+      a.uh[2 * e + 1] = sk ? hi[q] : 0.0;
+    }
+  }
+}
+
 }  // namespace skf
 
 namespace skf {
@@ -582,11 +779,12 @@ namespace skf {
 // a fixed order: deterministic, no atomics.  Self pairs are evaluated once as
 // before.
 //
-// Lane layout per warp (64 rows of A): lane = 8 ls + lr; lane (lr, ls) owns
-// rows wrow0 + lr + 8k (k < 8, packed in pairs k = 2p, 2p+1) and the sources
-// j = t0 + ls + 4g of each tile.  Row sums are combined across the 4 ls lanes
-// at the end; a source's B-side sum is combined across the 8 lr lanes with 3
-// shuffles, then across the 4 warps through shared memory.
+// Lane layout per warp (64 rows of A): lane = 16 ls + lr; lane (lr, ls) owns
+// rows wrow0 + lr + 16k (k < 4, packed in pairs (0,1), (2,3)) and the
+// sources j = t0 + ls + 2g of each tile.  Row sums are combined across the 2
+// ls lanes at the end; a source's B-side sums (one per lane, over its 4
+// rows) go to a padded shared tile and are added over the 16 lr lanes and
+// the 4 warps after the tile.
 struct SymArgs {
   const int32_t* work_box;
   const int32_t* work_row;

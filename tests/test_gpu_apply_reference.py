@@ -72,10 +72,11 @@ def test_host_and_device_apply_agree():
     assert np.array_equal(y2, y_host)
 
 
-@pytest.mark.parametrize("name", ["lap2d_square", "lap2d_annulus", "lap3d_cube", "lap3d_sphere"])
+@pytest.mark.parametrize("name", ["lap2d_square", "lap2d_annulus", "lap3d_cube", "lap3d_sphere", "helm3d_sphere"])
 def test_packed_and_scalar_mixed_kernels_agree(name):
-    """The packed FP32x2 Laplace kernel and the scalar FP32 kernel perform the
-    same per-pair arithmetic; only the summation grouping differs."""
+    """The packed FP32x2 kernels (Laplace, Helmholtz 3D) and the scalar FP32
+    kernel perform the same per-pair arithmetic; only the summation grouping
+    differs."""
     from skelfmm_gb300 import _lib
 
     d, plan = _plan(name)
