@@ -124,7 +124,6 @@ struct SkelArgs {
   double resid_tol;
   double* resid;    // [nbox] residual of the randomized ID (-1: not tried)
   int8_t* status;   // [nbox] 0 full QR; else 10 * sketch rounds + (1 kept, 2 rejected)
-  int64_t ycap;     // doubles of dynamic shared memory for the sketch (0: none)
   const int32_t* sk_tab;  // [sk_rows * rho] sketch entries: proxy row | sign bit 31
   const int32_t* order;  // block -> box of the batch, longest first (NULL: identity)
 };
@@ -464,158 +463,6 @@ __device__ int pivoted_qr(double* A, int m, int n, double tol, int kfix, const Q
   return rank;
 }
 
-// Column-pivoted Householder QR of a small real matrix held in shared memory
-// (s x n, leading dimension ld, n <= blockDim.x): thread j owns column j, so
-// the trailing update needs no cross-lane reduction per column (the FP64
-// pipe, not latency, bounds these factorizations).  Same pivoting, stopping
-// rule, squared-norm downdate and outputs as pivoted_qr (tol rule only).
-__device__ int pivoted_qr_smem(double* Y, int ld, int s, int n, double tol, const QrScratch& q) {
-  __shared__ int s_p;
-  __shared__ double s_h[4];
-  double* vn1 = q.vn1;
-  double* vn2 = q.vn2;
-  double* vv = q.vv;
-  double* red = q.red;
-  int* piv = q.piv;
-  const int j = threadIdx.x;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (j < n) {
-    const double* col = Y + (int64_t)j * ld;
-    double a0 = 0, a1 = 0;
-    int i = 0;
-    for (; i + 1 < s; i += 2) {
-      a0 = fma(col[i], col[i], a0);
-      a1 = fma(col[i + 1], col[i + 1], a1);
-    }
-    if (i < s) a0 = fma(col[i], col[i], a0);
-    vn1[j] = a0 + a1;
-    vn2[j] = a0 + a1;
-    piv[j] = j;
-  }
-  __syncthreads();
-  const int kmax = min(s, n);
-  const double tol3z = sqrt(2.220446049250313e-16);
-  double r00 = 0.0;
-  int rank = 0;
-  for (int k = 0; k < kmax; ++k) {
-    // pivot: first index of the largest squared partial norm
-    double best = -1.0;
-    int bi = n;
-    if (j >= k && j < n) {
-      best = vn1[j];
-      bi = j;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ob > best || (ob == best && oi < bi)) {
-        best = ob;
-        bi = oi;
-      }
-    }
-    if (lane == 0) {
-      red[warp] = best;
-      reinterpret_cast<int*>(red + 32)[warp] = bi;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double bb = red[0];
-      int bj = reinterpret_cast<int*>(red + 32)[0];
-      for (int w = 1; w < nw; ++w) {
-        const double ob = red[w];
-        const int oi = reinterpret_cast<int*>(red + 32)[w];
-        if (ob > bb || (ob == bb && oi < bj)) {
-          bb = ob;
-          bj = oi;
-        }
-      }
-      s_p = bj;
-    }
-    __syncthreads();
-    const int p = s_p;
-    if (p != k) {
-      for (int i = threadIdx.x; i < s; i += blockDim.x) {
-        const double t = Y[(int64_t)k * ld + i];
-        Y[(int64_t)k * ld + i] = Y[(int64_t)p * ld + i];
-        Y[(int64_t)p * ld + i] = t;
-      }
-      if (threadIdx.x == 0) {
-        const int t = piv[k];
-        piv[k] = piv[p];
-        piv[p] = t;
-        const double t1 = vn1[k], t2 = vn2[k];
-        vn1[k] = vn1[p];
-        vn2[k] = vn2[p];
-        vn1[p] = t1;
-        vn2[p] = t2;
-      }
-    }
-    __syncthreads();
-    // Householder reflector of column k (real zlarfg form)
-    const double* ck = Y + (int64_t)k * ld;
-    double sq = 0;
-    for (int i = k + 1 + threadIdx.x; i < s; i += blockDim.x) sq = fma(ck[i], ck[i], sq);
-    const double xnorm2 = block_sum(sq, red);
-    if (threadIdx.x == 0) {
-      const double ar = ck[k];
-      double beta = ar, tau = 0, scl = 0;
-      if (xnorm2 != 0.0) {
-        const double nrm = sqrt(ar * ar + xnorm2);
-        beta = ar >= 0 ? -nrm : nrm;
-        tau = (beta - ar) / beta;
-        scl = 1.0 / (ar - beta);
-      }
-      s_h[0] = beta;
-      s_h[1] = tau;
-      s_h[2] = scl;
-    }
-    __syncthreads();
-    const double beta = s_h[0], tau = s_h[1], scl = s_h[2];
-    if (k == 0) r00 = fabs(beta);
-    if (!(fabs(beta) > tol * r00) || r00 == 0.0) {
-      rank = k;
-      break;
-    }
-    rank = k + 1;
-    for (int i = k + threadIdx.x; i < s; i += blockDim.x) vv[i] = (i == k) ? 1.0 : ck[i] * scl;
-    __syncthreads();
-    if (threadIdx.x == 0) Y[(int64_t)k * ld + k] = beta;
-    // trailing update of the thread's own column
-    if (j > k && j < n) {
-      double* cj = Y + (int64_t)j * ld;
-      double w0 = 0, w1 = 0;
-      int i = k;
-      for (; i + 1 < s; i += 2) {
-        w0 = fma(vv[i], cj[i], w0);
-        w1 = fma(vv[i + 1], cj[i + 1], w1);
-      }
-      if (i < s) w0 = fma(vv[i], cj[i], w0);
-      const double f = tau * (w0 + w1);
-      for (i = k; i < s; ++i) cj[i] = fma(-f, vv[i], cj[i]);
-      const double akj2 = cj[k] * cj[k];
-      const double v1 = vn1[j];
-      const double rem = v1 - akj2;
-      if (v1 != 0.0) {
-        if (rem <= tol3z * vn2[j]) {
-          double p0 = 0, p1 = 0;
-          for (i = k + 1; i + 1 < s; i += 2) {
-            p0 = fma(cj[i], cj[i], p0);
-            p1 = fma(cj[i + 1], cj[i + 1], p1);
-          }
-          if (i < s) p0 = fma(cj[i], cj[i], p0);
-          vn1[j] = p0 + p1;
-          vn2[j] = p0 + p1;
-        } else {
-          vn1[j] = rem;
-        }
-      }
-    }
-    __syncthreads();
-  }
-  __syncthreads();
-  return rank;
-}
-
 // T = R11^{-1} R12 (row-major rank x (n - rank)) from the R that pivoted_qr
 // left in A: column back substitution, one warp per right-hand side.
 template <int OP>
@@ -690,14 +537,13 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? (RAND ? 3 : 2) : 1) k_skel_box
   // randomized ID while the sketch is well below the proxy matrix
   int s = kp > 0 ? kp + a.oversample : 0;
   const bool sketch = kp > 0 && 2 * s <= m && kp < n;
-  // smem: vn1[n], vn2[n], v[m * W], red[64], sketch[ycap], piv[n]
+  // smem: vn1[n], vn2[n], v[m * W], red[64], piv[n]
   QrScratch q;
   q.vn1 = sm;
   q.vn2 = q.vn1 + n;
   q.vv = q.vn2 + n;
   q.red = q.vv + (size_t)m * W;
-  double* sY = q.red + 64;
-  q.piv = reinterpret_cast<int*>(sY + a.ycap);
+  q.piv = reinterpret_cast<int*>(q.red + 64);
 
   double* A = a.ws + a.ws_off[lb];
   double c[3] = {0, 0, 0};
@@ -719,16 +565,11 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? (RAND ? 3 : 2) : 1) k_skel_box
   if (sketch) {
     // ---- 2a. sketches Y = S K (s x n, after K in the workspace): row t of
     // S has rho entries +-1 at hashed proxy rows; doubled while saturated
-    double* gY = A + (int64_t)m * n * W;
-    double* Y = gY;
+    double* Y = A + (int64_t)m * n * W;
     const int guard = max(2, a.oversample / 2);
     bool ok = false;
     const int rounds = 1;
     {
-      // a real sketch that fits in shared memory is factored there, one
-      // thread per column
-      const bool in_smem = !C && n <= (int)blockDim.x && (int64_t)s * n <= a.ycap;
-      Y = in_smem ? sY : gY;
       for (int64_t idx = threadIdx.x; idx < (int64_t)s * n; idx += blockDim.x) {
         const int j = (int)(idx / s), t = (int)(idx % s);
         double yr = 0, yi = 0;
@@ -749,7 +590,7 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? (RAND ? 3 : 2) : 1) k_skel_box
         if (C) Y[((int64_t)j * s + t) * W + 1] = yi;
       }
       __syncthreads();
-      rank = in_smem ? pivoted_qr_smem(Y, s, s, n, a.sketch_tol, q) : pivoted_qr<OP>(Y, s, n, a.sketch_tol, 0, q);
+      rank = pivoted_qr<OP>(Y, s, n, a.sketch_tol, 0, q);
       ok = !(rank < n && rank > s - guard);  // saturated: the sketch hides rank
     }
     if (ok) {
@@ -1097,8 +938,7 @@ template <int OP>
 static int launch_skel(SkelArgs a, int nbox, int maxn, int maxm, cudaStream_t st, int nbig = 0,
                        cudaStream_t side = nullptr, cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
   constexpr int W = OpTraits<OP>::kComplex ? 2 : 1;
-  const size_t smem =
-      sizeof(double) * ((size_t)2 * maxn + (size_t)maxm * W + 64 + (size_t)a.ycap) + sizeof(int) * (size_t)maxn;
+  const size_t smem = sizeof(double) * ((size_t)2 * maxn + (size_t)maxm * W + 64) + sizeof(int) * (size_t)maxn;
   if (smem > 200 * 1024) return SKF_ERR_UNSUPPORTED;
   if (nbig <= 0 || nbig >= nbox || !side || !a.order) return launch_skel_nt<OP, kSkelThreads>(a, nbox, smem, st);
   SKF_CUDA_TRY(cudaEventRecord(e0, st));
@@ -1158,7 +998,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     const int64_t n = hoff[b + 1] - hoff[b];
     if (!ra.kpred || hk[b] <= 0) return mrows;
     const int64_t s = (int64_t)hk[b] + ra.oversample;
-    return (2 * s <= mrows && hk[b] < n) ? mrows + mrows / 2 : mrows;  // K and the largest sketch
+    return (2 * s <= mrows && hk[b] < n) ? mrows + s : mrows;  // K and the sketch
   };
 
   double* dtmpl = nullptr;
@@ -1278,18 +1118,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     a.resid = ra.resid;
     a.status = ra.status;
     int maxn_batch = 1;
-    int64_t ymax = 0;
-    for (int b = b0; b < b1; ++b) {
-      const int64_t n = hoff[b + 1] - hoff[b];
-      maxn_batch = std::max<int>(maxn_batch, (int)n);
-      if (ra.kpred && hk[b] > 0 && 2 * ((int64_t)hk[b] + ra.oversample) <= mrows && hk[b] < n)
-        ymax = std::max<int64_t>(ymax, ((int64_t)hk[b] + ra.oversample) * n * W);
-    }
-    // sketches are factored in global memory by the warp-per-column QR with
-    // register-resident columns (faster than the shared-memory
-    // thread-per-column QR, pivoted_qr_smem, at these sizes)
-    a.ycap = 0;
-    (void)ymax;
+    for (int b = b0; b < b1; ++b) maxn_batch = std::max<int>(maxn_batch, (int)(hoff[b + 1] - hoff[b]));
     if (status == SKF_OK) {
       switch (op) {
 #define SKF_CASE(OPID) \
