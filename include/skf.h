@@ -242,6 +242,16 @@ int skf_mlp_train_step(int32_t nin, float* theta, void* theta16, const void* x16
                        float* scratch, float* grad, float* adam_m, float* adam_v, int32_t step, float lr,
                        float beta1, float beta2, float eps, int32_t apply, float* loss, void* stream);
 
+/*
+ * Geometric features of the rank network: for box b the points
+ * x[off[b] .. off[b+1]) (row-major [.. x ndim], ndim 2 or 3) relative to
+ * centers[b], in units of `width`: out[9 b + 0..2] their mean, out[9 b +
+ * 3..8] their second central moments (xx yy zz xy xz yz; z terms 0 in 2D).
+ * All pointers DEVICE; one block per box.
+ */
+int skf_box_moments(int32_t nbox, int32_t ndim, const int64_t* off, const double* x, const double* centers,
+                    double width, double* out, void* stream);
+
 const char* skf_status_string(int32_t status);
 int skf_version(void);
 

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <random>
+#include <type_traits>
 #include <vector>
 
 #include "skf_internal.cuh"
@@ -126,6 +127,9 @@ struct SkelArgs {
   int8_t* status;   // [nbox] 0 full QR; else 10 * sketch rounds + (1 kept, 2 rejected)
   const int32_t* sk_tab;  // [sk_rows * rho] sketch entries: proxy row | sign bit 31
   const int32_t* order;  // block -> box of the batch, longest first (NULL: identity)
+  // deferred fallback: a rejected randomized ID writes only its status and
+  // residual; its pivoted-QR ID runs in a second launch over the rejects
+  int defer;
 };
 
 constexpr int kSkelThreads = 256;
@@ -192,41 +196,133 @@ struct QrScratch {
   int* piv;     // [n] column permutation
 };
 
-// One warp applies the real reflector I - tau v v^T to rows k..m-1 of the
-// column cj (m - k <= 32 * kColRegs): the column slice is loaded into
-// registers with every load in flight, so a step costs one round trip to L2
-// per column instead of one per 32 rows.  Returns the squared norm of rows
-// > k after the update in `part` and the updated row-k entry in `akj`.
+// Real reflector I - tau v v^T on rows k..m-1 of columns held in registers.
+// A group of G lanes (G = 8, 16 or 32, group lane sl) holds one column, CR
+// rows per lane (row k + sl + G q, m - k <= G CR), loaded with every load in
+// flight: a step costs one round trip to L2 per column.  The narrowest group
+// whose registers hold the slice is used, so the FP64 instructions issued per
+// column follow the slice length (a short sketch column takes a quarter of a
+// warp) instead of the register capacity.
 constexpr int kColRegs = 24;
-__device__ __forceinline__ void warp_reflect_column(double* __restrict__ cj, const double* __restrict__ vv, int k,
-                                                    int m, double tau, int lane, double& part, double& akj) {
-  double cr[kColRegs];
+
+// Applies the reflector to the group's column (live: the group has a
+// column); returns its updated row-k entry on every lane of the group.
+template <int G, int CR>
+__device__ __forceinline__ double group_reflect(double* __restrict__ cj, bool live, const double* __restrict__ vv,
+                                                int k, int m, double tau, int sl, double (&cr)[CR]) {
 #pragma unroll
-  for (int q = 0; q < kColRegs; ++q) {
-    const int i = k + lane + 32 * q;
-    cr[q] = (i < m) ? cj[i] : 0.0;
+  for (int q = 0; q < CR; ++q) {
+    const int i = k + sl + G * q;
+    cr[q] = (live && i < m) ? cj[i] : 0.0;
   }
   double w0 = 0, w1 = 0;
 #pragma unroll
-  for (int q = 0; q < kColRegs; q += 2) {
-    const int i = k + lane + 32 * q;
-    if (i < m) w0 = fma(vv[i], cr[q], w0);
-    if (i + 32 < m) w1 = fma(vv[i + 32], cr[q + 1], w1);
+  for (int q = 0; q < CR; q += 2) {
+    const int i = k + sl + G * q;
+    w0 = fma(i < m ? vv[i] : 0.0, cr[q], w0);
+    if (q + 1 < CR) w1 = fma(i + G < m ? vv[i + G] : 0.0, cr[q + 1], w1);
   }
-  const double f = tau * warp_sum_d(w0 + w1);
-  double p = 0;
+  double w = w0 + w1;
 #pragma unroll
-  for (int q = 0; q < kColRegs; ++q) {
-    const int i = k + lane + 32 * q;
+  for (int o = G / 2; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+  const double f = tau * w;
+#pragma unroll
+  for (int q = 0; q < CR; ++q) {
+    const int i = k + sl + G * q;
     if (i < m) {
       const double v = fma(-vv[i], f, cr[q]);
       cr[q] = v;
-      cj[i] = v;
-      if (i > k) p = fma(v, v, p);
+      if (live) cj[i] = v;
     }
   }
-  part = p;
-  akj = __shfl_sync(0xffffffffu, cr[0], 0);
+  const int lane = threadIdx.x & 31;
+  return __shfl_sync(0xffffffffu, cr[0], lane - sl);
+}
+
+// Squared norm of rows > k of the group's updated column (group-reduced).
+template <int G, int CR>
+__device__ __forceinline__ double group_norm_below(const double (&cr)[CR], int k, int m, int sl) {
+  double p = 0;
+#pragma unroll
+  for (int q = 0; q < CR; ++q) {
+    const int i = k + sl + G * q;
+    if (i > k && i < m) p = fma(cr[q], cr[q], p);
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+  return p;
+}
+
+// Partial-norm downdate of column j after step k (LAWN 176, squared form):
+// vn1 - |r_kj|^2, recomputed from the column when it falls to
+// sqrt(eps) vn2.  `norm()` is evaluated by the whole warp only when some
+// group of the warp recomputes.
+template <typename NormFn>
+__device__ __forceinline__ void downdate_norm(bool live, int j, bool lead, double akj, double* vn1, double* vn2,
+                                              double tol3z, NormFn norm) {
+  double v1 = 0.0, rem = 0.0;
+  bool rc = false;
+  if (live) {
+    v1 = vn1[j];
+    rem = v1 - akj * akj;
+    rc = v1 != 0.0 && rem <= tol3z * vn2[j];
+  }
+  double p = 0.0;
+  if (__any_sync(0xffffffffu, rc)) p = norm();
+  if (live && lead) {
+    if (rc) {
+      vn1[j] = p;
+      vn2[j] = p;
+    } else if (v1 != 0.0) {
+      vn1[j] = rem;
+    }
+  }
+}
+
+// Trailing update of columns k+1..n-1 of the column-major m x n matrix A,
+// 32 / G columns per warp pass.
+template <int G, int CR>
+__device__ __noinline__ void reflect_trailing(double* A, int m, int n, int k, const double* __restrict__ vv, double tau,
+                                 double* vn1, double* vn2, double tol3z) {
+  constexpr int NG = 32 / G;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int g = lane / G, sl = lane - g * G;
+  for (int j0 = k + 1 + NG * warp; j0 < n; j0 += NG * nw) {
+    const int j = j0 + g;
+    const bool live = j < n;
+    double cr[CR];
+    const double akj = group_reflect<G, CR>(A + (int64_t)(live ? j : j0) * m, live, vv, k, m, tau, sl, cr);
+    downdate_norm(live, j, sl == 0, akj, vn1, vn2, tol3z, [&] { return group_norm_below<G, CR>(cr, k, m, sl); });
+  }
+}
+
+// Picks the lane group and register count for rows k..m-1; false when the
+// slice exceeds 32 kColRegs rows.
+__device__ __forceinline__ bool reflect_trailing_regs(double* A, int m, int n, int k, const double* vv, double tau,
+                                                      double* vn1, double* vn2, double tol3z) {
+  const int len = m - k;
+  if (len <= 8 * kColRegs) {
+    const int cr = (len + 7) / 8;
+    if (cr <= 4) reflect_trailing<8, 4>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 8) reflect_trailing<8, 8>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 12) reflect_trailing<8, 12>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 16) reflect_trailing<8, 16>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 20) reflect_trailing<8, 20>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else reflect_trailing<8, 24>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+  } else if (len <= 16 * kColRegs) {
+    const int cr = (len + 15) / 16;
+    if (cr <= 16) reflect_trailing<16, 16>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 20) reflect_trailing<16, 20>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else reflect_trailing<16, 24>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+  } else if (len <= 32 * kColRegs) {
+    const int cr = (len + 31) / 32;
+    if (cr <= 16) reflect_trailing<32, 16>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 20) reflect_trailing<32, 20>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else reflect_trailing<32, 24>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+  } else {
+    return false;
+  }
+  return true;
 }
 
 // Column-pivoted Householder QR of the m x n column-major matrix A (leading
@@ -387,26 +483,11 @@ __device__ int pivoted_qr(double* A, int m, int n, double tol, int kfix, const Q
       if (C) ck[k * W + 1] = 0.0;
     }
     // trailing update: A(k:, j) -= conj(tau) v (v^H A(k:, j)), one warp per column
-    if (!C && m - k <= 32 * kColRegs) {
-      for (int j = k + 1 + warp; j < n; j += nw) {
-        double part, akj;
-        warp_reflect_column(A + (int64_t)j * m, vv, k, m, taur, lane, part, akj);
-        const double v1 = vn1[j];
-        const double rem = v1 - akj * akj;
-        const bool recompute = v1 != 0.0 && rem <= tol3z * vn2[j];
-        if (recompute) {
-          part = warp_sum_d(part);
-          if (lane == 0) {
-            vn1[j] = part;
-            vn2[j] = part;
-          }
-        } else if (lane == 0 && v1 != 0.0) {
-          vn1[j] = rem;
-        }
-        __syncwarp();
+    if constexpr (!C) {
+      if (reflect_trailing_regs(A, m, n, k, vv, taur, vn1, vn2, tol3z)) {
+        __syncthreads();
+        continue;
       }
-      __syncthreads();
-      continue;
     }
     for (int j = k + 1 + warp; j < n; j += nw) {
       double* cj = A + (int64_t)j * m * W;
@@ -520,10 +601,9 @@ __device__ void write_T(double* A, int m, int n, int rank, double* T, double* ri
   __syncthreads();
 }
 
-// RAND: the launch carries randomized boxes (a.kpred); that variant keeps
-// three blocks per SM for its latency-bound sketch factorizations.
+// RAND: the launch carries randomized boxes (a.kpred).
 template <int OP, int NT, bool RAND>
-__global__ void __launch_bounds__(NT, NT <= 256 ? (RAND ? 3 : 2) : 1) k_skel_box(SkelArgs a) {
+__global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) {
   constexpr bool C = OpTraits<OP>::kComplex;
   constexpr int D = OpTraits<OP>::kDim;
   constexpr int W = C ? 2 : 1;  // scalars per matrix entry
@@ -549,13 +629,20 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? (RAND ? 3 : 2) : 1) k_skel_box
   double c[3] = {0, 0, 0};
   for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
 
-  // ---- 1. proxy matrix, column j = box point j
-  for (int64_t idx = threadIdx.x; idx < (int64_t)m * n; idx += blockDim.x) {
-    const int j = (int)(idx / m), i = (int)(idx % m);
-    double kr, ki;
-    proxy_entry<OP>(a, c, i, a.x + (off + j) * D, a.geom ? a.geom + (off + j) * 3 : nullptr, kr, ki);
-    A[((int64_t)j * m + i) * W] = kr;
-    if (C) A[((int64_t)j * m + i) * W + 1] = ki;
+  // ---- 1. proxy matrix, column j = box point j (a warp per column)
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < n; j += nw) {
+      const double* xj = a.x + (off + j) * D;
+      const double* gj = a.geom ? a.geom + (off + j) * 3 : nullptr;
+      double* col = A + (int64_t)j * m * W;
+      for (int i = lane; i < m; i += 32) {
+        double kr, ki;
+        proxy_entry<OP>(a, c, i, xj, gj, kr, ki);
+        col[i * W] = kr;
+        if (C) col[i * W + 1] = ki;
+      }
+    }
   }
   __syncthreads();
 
@@ -633,6 +720,7 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? (RAND ? 3 : 2) : 1) k_skel_box
     if (a.status) a.status[b] = 0;
   }
   if (!done) {
+    if (a.defer) return;
     // ---- 3. full column-pivoted QR ID of K
     rank = pivoted_qr<OP>(A, m, n, a.tol >= 1.0 ? 0.0 : a.tol, a.tol >= 1.0 ? (int)a.tol : 0, q);
     write_T<OP>(A, m, n, rank, T, q.vn1);
@@ -689,14 +777,17 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
   double c[3] = {0, 0, 0};
   for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
 
-  // ---- proxy matrix, owned columns only
-  for (int64_t idx = threadIdx.x; idx < (int64_t)m * ncl; idx += blockDim.x) {
-    const int jl = (int)(idx / m), i = (int)(idx % m);
+  // ---- proxy matrix, owned columns only (a warp per column)
+  for (int jl = warp; jl < ncl; jl += nw) {
     const int j = cr + NC * jl;
     if (j >= n) continue;
-    double kr, ki;
-    proxy_entry<OP>(a, c, i, a.x + (off + j) * D, a.geom ? a.geom + (off + j) * 3 : nullptr, kr, ki);
-    A[(int64_t)j * m + i] = kr;
+    const double* xj = a.x + (off + j) * D;
+    const double* gj = a.geom ? a.geom + (off + j) * 3 : nullptr;
+    for (int i = lane; i < m; i += 32) {
+      double kr, ki;
+      proxy_entry<OP>(a, c, i, xj, gj, kr, ki);
+      A[(int64_t)j * m + i] = kr;
+    }
   }
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     piv[j] = j;
@@ -829,40 +920,48 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
     const double* ov = cl.map_shared_rank(vsh, owner);
     for (int i = k + threadIdx.x; i < m; i += blockDim.x) vloc[i] = ov[i];
     __syncthreads();
-    // ---- trailing update of the owned columns at positions > k
-    for (int jl = warp; jl < ncl; jl += nw) {
-      const int j = cr + NC * jl;
-      if (j >= n || posof[j] <= k) continue;
-      double* cj = A + (int64_t)j * m;
-      double part = 0, akj;
-      if (m - k <= 32 * kColRegs) {
-        warp_reflect_column(cj, vloc, k, m, tau, lane, part, akj);
-      } else {
+    // ---- trailing update of the owned columns at positions > k (one warp
+    // per column, register count by the slice length)
+    auto update_regs = [&](auto regs) {
+      constexpr int CRN = decltype(regs)::value;
+      for (int jl = warp; jl < ncl; jl += nw) {
+        const int j = cr + NC * jl;
+        if (j >= n || posof[j] <= k) continue;
+        double c[CRN];
+        const double akj = group_reflect<32, CRN>(A + (int64_t)j * m, true, vloc, k, m, tau, lane, c);
+        downdate_norm(true, jl, lane == 0, akj, vn1, vn2, tol3z,
+                      [&] { return group_norm_below<32, CRN>(c, k, m, lane); });
+      }
+    };
+    const int len = m - k;
+    if (len <= 32 * 8) {
+      update_regs(std::integral_constant<int, 8>());
+    } else if (len <= 32 * 16) {
+      update_regs(std::integral_constant<int, 16>());
+    } else if (len <= 32 * 20) {
+      update_regs(std::integral_constant<int, 20>());
+    } else if (len <= 32 * kColRegs) {
+      update_regs(std::integral_constant<int, kColRegs>());
+    } else {
+      for (int jl = warp; jl < ncl; jl += nw) {
+        const int j = cr + NC * jl;
+        if (j >= n || posof[j] <= k) continue;
+        double* cj = A + (int64_t)j * m;
         double w = 0;
         for (int i = k + lane; i < m; i += 32) w += vloc[i] * cj[i];
         w = warp_sum_d(w);
         const double f = tau * w;
+        double part = 0;
         for (int i = k + lane; i < m; i += 32) {
           const double v = cj[i] - vloc[i] * f;
           cj[i] = v;
           if (i > k) part += v * v;
         }
         __syncwarp();
-        akj = cj[k];
+        const double akj = cj[k];
+        downdate_norm(true, jl, lane == 0, akj, vn1, vn2, tol3z, [&] { return warp_sum_d(part); });
+        __syncwarp();
       }
-      const double v1 = vn1[jl];
-      const double rem = v1 - akj * akj;
-      const bool recompute = v1 != 0.0 && rem <= tol3z * vn2[jl];
-      if (recompute) {
-        part = warp_sum_d(part);
-        if (lane == 0) {
-          vn1[jl] = part;
-          vn2[jl] = part;
-        }
-      } else if (lane == 0 && v1 != 0.0) {
-        vn1[jl] = rem;
-      }
-      __syncwarp();
     }
     __syncthreads();
   }
@@ -900,6 +999,11 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
     }
     for (int i = lane; i < rank; i += 32) T[(int64_t)i * nr + cidx] = bcol[i];
   }
+}
+
+__global__ void k_fill_f64(double* __restrict__ p, int n, double v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
 }
 
 template <int OP>
@@ -1023,6 +1127,22 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     SKF_CUDA_TRY(cudaMemcpyAsync(dtab, tab.data(), sizeof(int32_t) * tab.size(), cudaMemcpyHostToDevice, st));
   }
 
+  // every box reports status 0 and residual -1 unless its randomized ID is
+  // tried; the status also drives the second (pivoted-QR) launch
+  int8_t* dstat = ra.status;
+  int8_t* own_stat = nullptr;
+  if (ra.kpred && nbox > 0) {
+    if (!dstat) {
+      SKF_CUDA_TRY(cudaMallocAsync(&own_stat, (size_t)nbox, st));
+      dstat = own_stat;
+    }
+    SKF_CUDA_TRY(cudaMemsetAsync(dstat, 0, (size_t)nbox, st));
+    if (ra.resid) {
+      k_fill_f64<<<(nbox + 255) / 256, 256, 0, st>>>(ra.resid, nbox, -1.0);
+      SKF_CUDA_TRY(cudaGetLastError());
+    }
+  }
+
   // workspace in batches of boxes bounded by ~4 GiB
   const int64_t budget = (int64_t)4 << 30;
   int status = SKF_OK;
@@ -1040,40 +1160,25 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
       acc += need;
       ++b1;
     }
-    // longest box first (cost ~ rows x n x min(rows, n)) so the tail of the
-    // launch holds the small boxes
-    std::vector<int32_t> ord(b1 - b0);
-    std::vector<double> cost(b1 - b0);
-    for (int b = b0; b < b1; ++b) {
+    // Boxes of the batch whose randomized ID is tried (sketch well below the
+    // proxy matrix); the others take the pivoted-QR ID directly.
+    auto sketched = [&](int b) {
+      return ra.kpred && hk[b] > 0 && 2 * ((int64_t)hk[b] + ra.oversample) <= mrows &&
+             hk[b] < hoff[b + 1] - hoff[b];
+    };
+    // cost ~ rows x n x min(rows, n), rows = the sketch or the proxy matrix
+    auto box_cost = [&](int b, bool sketch) {
       const double n = (double)(hoff[b + 1] - hoff[b]);
-      double rows = mrows;
-      if (ra.kpred && hk[b] > 0 && 2 * ((int64_t)hk[b] + ra.oversample) <= mrows && hk[b] < n)
-        rows = (double)hk[b] + ra.oversample;
-      cost[b - b0] = rows * n * std::min(rows, n);
-      ord[b - b0] = b - b0;
-    }
-    std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
-    // boxes far above an even share of the batch's work get a 1024-thread block
-    double total = 0.0;
-    for (double c : cost) total += c;
-    const double share = total / (152.0 * 4.0);
-    int nbig = 0;
-    // (real operators: a cluster per box from twice an even share)
-    const double big = (W == 1 ? 2.0 : 4.0) * share;
-    while (nbig < (int)ord.size() && cost[ord[nbig]] > big && hoff[b0 + ord[nbig] + 1] - hoff[b0 + ord[nbig]] >= 192)
-      ++nbig;
-    if (nbig > 0 && !side) {
-      if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
-          cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming) != cudaSuccess ||
-          cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming) != cudaSuccess)
-        nbig = 0;
-    }
+      const double rows = sketch ? (double)hk[b] + ra.oversample : (double)mrows;
+      return rows * n * std::min(rows, n);
+    };
     double* ws = nullptr;
     int64_t* dwso = nullptr;
     int32_t* dord = nullptr;
+    const size_t nb = (size_t)(b1 - b0);
     cudaError_t e = cudaMallocAsync(&ws, std::max<int64_t>(acc, 8), st);
     if (e == cudaSuccess) e = cudaMallocAsync(&dwso, sizeof(int64_t) * wso.size(), st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&dord, sizeof(int32_t) * ord.size(), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dord, sizeof(int32_t) * 2 * nb, st);
     if (e != cudaSuccess) {
       set_last_cuda_error(e);
       status = SKF_ERR_OOM;
@@ -1082,14 +1187,11 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
       break;
     }
     e = cudaMemcpyAsync(dwso, wso.data(), sizeof(int64_t) * wso.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(dord, ord.data(), sizeof(int32_t) * ord.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) {
       set_last_cuda_error(e);
       status = SKF_ERR_CUDA;
     }
     SkelArgs a{};
-    a.order = dord;
     a.off = off;
     a.x = x;
     a.geom = geom;
@@ -1107,7 +1209,6 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     a.t_off_out = t_off_out;
     a.t_out = static_cast<double*>(t_out);
     a.first_box = b0;
-    a.kpred = ra.kpred;
     a.sk_tab = dtab;
     a.oversample = ra.oversample;
     a.rho = ra.rho;
@@ -1115,14 +1216,42 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     a.nchk = ra.nchk;
     a.sketch_tol = ra.sketch_tol;
     a.resid_tol = ra.resid_tol;
-    a.resid = ra.resid;
-    a.status = ra.status;
     int maxn_batch = 1;
     for (int b = b0; b < b1; ++b) maxn_batch = std::max<int>(maxn_batch, (int)(hoff[b + 1] - hoff[b]));
-    if (status == SKF_OK) {
+    // Launches the boxes `list` (batch-local) longest first; boxes far above
+    // an even share of the launch's work get a thread-block cluster (real
+    // operators, from twice an even share) or a 1024-thread block on `side`.
+    auto launch_list = [&](SkelArgs la, std::vector<int32_t> list, bool sketch, int32_t* dlist) -> int {
+      if (list.empty()) return SKF_OK;
+      std::vector<double> cost(list.size());
+      for (size_t i = 0; i < list.size(); ++i) cost[i] = box_cost(b0 + list[i], sketch);
+      std::vector<int32_t> idx(list.size());
+      for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int32_t)i;
+      std::stable_sort(idx.begin(), idx.end(), [&](int32_t p, int32_t q) { return cost[p] > cost[q]; });
+      std::vector<int32_t> ord(list.size());
+      double total = 0.0;
+      for (size_t i = 0; i < idx.size(); ++i) {
+        ord[i] = list[idx[i]];
+        total += cost[idx[i]];
+      }
+      // (in a randomized launch the big boxes of real operators take the
+      // clustered pivoted-QR ID: 8 SMs on the full matrix beat one block on
+      // the sketch)
+      int nbig = 0;
+      const double big = (W == 1 ? 2.0 : 4.0) * total / (152.0 * 4.0);
+      while (nbig < (int)ord.size() && cost[idx[nbig]] > big && hoff[b0 + ord[nbig] + 1] - hoff[b0 + ord[nbig]] >= 192)
+        ++nbig;
+      if (nbig > 0 && !side) {
+        if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming) != cudaSuccess)
+          nbig = 0;
+      }
+      SKF_CUDA_TRY(cudaMemcpyAsync(dlist, ord.data(), sizeof(int32_t) * ord.size(), cudaMemcpyHostToDevice, st));
+      la.order = dlist;
       switch (op) {
 #define SKF_CASE(OPID) \
-  case OPID: status = launch_skel<OPID>(a, b1 - b0, maxn_batch, mrows, st, nbig, side, ev0, ev1); break;
+  case OPID: return launch_skel<OPID>(la, (int)ord.size(), maxn_batch, mrows, st, nbig, side, ev0, ev1);
         SKF_CASE(SKF_LAPLACE_2D)
         SKF_CASE(SKF_LAPLACE_3D)
         SKF_CASE(SKF_HELMHOLTZ_2D)
@@ -1132,9 +1261,29 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
         SKF_CASE(SKF_HELMHOLTZ_DOUBLE_LAYER_3D)
         SKF_CASE(SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D)
 #undef SKF_CASE
-        default: status = SKF_ERR_ARG;
+        default: return SKF_ERR_ARG;
+      }
+    };
+    std::vector<int32_t> rnd, full;
+    for (int b = b0; b < b1; ++b) (sketched(b) ? rnd : full).push_back(b - b0);
+    if (status == SKF_OK && !rnd.empty()) {
+      // phase 1: randomized IDs; rejects only report their status
+      SkelArgs r = a;
+      r.kpred = ra.kpred;
+      r.resid = ra.resid;
+      r.status = dstat;
+      r.defer = 1;
+      status = launch_list(r, rnd, true, dord);
+      if (status == SKF_OK) {
+        std::vector<int8_t> hs(nb);
+        SKF_CUDA_TRY(cudaMemcpyAsync(hs.data(), dstat + b0, nb, cudaMemcpyDeviceToHost, st));
+        SKF_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int32_t lb : rnd)
+          if (hs[lb] % 10 == 2) full.push_back(lb);
       }
     }
+    // phase 2: pivoted-QR IDs of the other boxes and of the rejects
+    if (status == SKF_OK) status = launch_list(a, full, false, dord + nb);
     cudaFreeAsync(ws, st);
     cudaFreeAsync(dwso, st);
     cudaFreeAsync(dord, st);
@@ -1142,6 +1291,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
   }
   cudaFreeAsync(dtmpl, st);
   if (dtab) cudaFreeAsync(dtab, st);
+  if (own_stat) cudaFreeAsync(own_stat, st);
   if (side) {
     cudaStreamDestroy(side);
     cudaEventDestroy(ev0);

@@ -240,6 +240,68 @@ __global__ void k_f32_to_bf16(const float* __restrict__ a, __nv_bfloat16* __rest
     b[i] = __float2bfloat16_rn(a[i]);
 }
 
+// Geometric moments of the rank network's features: per box, the mean
+// offset of its points from the box centre and their second central
+// moments, in units of the box width.  One block per box, FP64 sums.
+// out[9 b ..]: mean x y z, then xx yy zz xy xz yz.
+constexpr int kMomThreads = 128;
+__global__ void __launch_bounds__(kMomThreads) k_box_moments(const int64_t* __restrict__ off,
+                                                             const double* __restrict__ x, int ndim,
+                                                             const double* __restrict__ centers, double width,
+                                                             double* __restrict__ out) {
+  const int b = blockIdx.x;
+  const int64_t o0 = off[b], o1 = off[b + 1];
+  double c[3] = {0.0, 0.0, 0.0};
+  for (int d = 0; d < ndim; ++d) c[d] = centers[(int64_t)b * ndim + d];
+  double s[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) s[q] = 0.0;
+  for (int64_t i = o0 + threadIdx.x; i < o1; i += kMomThreads) {
+    double r[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < ndim; ++d) r[d] = (x[i * ndim + d] - c[d]) / width;
+    s[0] += r[0];
+    s[1] += r[1];
+    s[2] += r[2];
+    s[3] += r[0] * r[0];
+    s[4] += r[1] * r[1];
+    s[5] += r[2] * r[2];
+    s[6] += r[0] * r[1];
+    s[7] += r[0] * r[2];
+    s[8] += r[1] * r[2];
+  }
+  __shared__ double red[kMomThreads / 32][9];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    double v = s[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[w][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 9) {
+    const int q = threadIdx.x;
+    double t = 0.0;
+    for (int k = 0; k < kMomThreads / 32; ++k) t += red[k][q];
+    red[0][q] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double n = o1 > o0 ? (double)(o1 - o0) : 1.0;
+    double m[3];
+    for (int d = 0; d < 3; ++d) m[d] = red[0][d] / n;
+    double* o = out + (int64_t)9 * b;
+    o[0] = m[0];
+    o[1] = m[1];
+    o[2] = m[2];
+    o[3] = red[0][3] / n - m[0] * m[0];
+    o[4] = red[0][4] / n - m[1] * m[1];
+    o[5] = red[0][5] / n - m[2] * m[2];
+    o[6] = red[0][6] / n - m[0] * m[1];
+    o[7] = red[0][7] / n - m[0] * m[2];
+    o[8] = red[0][8] / n - m[1] * m[2];
+  }
+}
+
 static int mlp_smem_attr(const void* fn) {
   const size_t bytes = mlp_smem_floats() * sizeof(float);
   SKF_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -299,6 +361,16 @@ int skf_mlp_train_step(int32_t nin, float* theta, void* theta16, const void* x16
   k_mlp_reduce_adam<<<(unsigned)((P + 1 + 255) / 256), 256, 0, st>>>(
       P, (int)tiles, scratch, grad, theta, static_cast<__nv_bfloat16*>(theta16), adam_m, adam_v, step, lr, beta1,
       beta2, eps, apply, n, loss);
+  SKF_CUDA_TRY(cudaGetLastError());
+  return SKF_OK;
+}
+
+int skf_box_moments(int32_t nbox, int32_t ndim, const int64_t* off, const double* x, const double* centers,
+                    double width, double* out, void* stream) {
+  if (nbox < 0 || (ndim != 2 && ndim != 3) || !(width > 0.0)) return SKF_ERR_ARG;
+  if (nbox == 0) return SKF_OK;
+  if (!off || !x || !centers || !out) return SKF_ERR_ARG;
+  k_box_moments<<<nbox, kMomThreads, 0, static_cast<cudaStream_t>(stream)>>>(off, x, ndim, centers, width, out);
   SKF_CUDA_TRY(cudaGetLastError());
   return SKF_OK;
 }

@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 
 import numpy as np
 import torch
@@ -31,14 +32,16 @@ DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "rank
 
 def level_features(fmm, lev, x_lev=None, off=None):
     """Features [nboxes_at_lev, NFEAT] (float32) of every box of ``lev`` from
-    its candidate points (the points its ID factors), computed on the host:
+    its candidate points (the points its ID factors):
 
     0 level, 1 log2(candidates + 1), 2 log2(proxy rows), 3 colleagues,
     4 children, 5 leaf flag, 6-8 mean offset from the centre / width,
     9-14 second central moments / width^2 (xx yy zz xy xz yz), 15 log10 tol,
     16 kappa * width, 17 3D flag, 18 complex-kernel flag, 19 geometry-kernel
     flag, 20 log2(points under the box + 1), 21 coarse neighbours.
-    ``x_lev`` is accepted for the predictor interface and not used.
+    Offsets and moments come from the library's ``skf_box_moments`` kernel
+    over ``x_lev`` (the level's candidate coordinates on the device, in
+    ``off`` segments; gathered from the build's device copy when None).
     """
     tree = fmm.tree
     ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
@@ -48,15 +51,9 @@ def level_features(fmm, lev, x_lev=None, off=None):
     bs = np.diff(off).astype(np.int64)
     d = tree.ndim
     w = float(tree.L0 * 0.5 ** lev)
-    seg = np.repeat(np.arange(nbl), bs)
-    rel = (tree.XX[fmm._ids[lev]] - tree._box_center[ls:le][seg]) / w
-    cnt = np.maximum(bs, 1).astype(np.float64)
-    s1 = np.stack([np.bincount(seg, weights=rel[:, i], minlength=nbl) for i in range(d)], 1) / cnt[:, None]
-    pairs = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
-    mom = np.zeros((nbl, 6))
-    for k, (i, j) in enumerate(pairs):
-        if i < d and j < d:
-            mom[:, k] = np.bincount(seg, weights=rel[:, i] * rel[:, j], minlength=nbl) / cnt - s1[:, i] * s1[:, j]
+    m9 = box_moments(fmm, lev, x_lev, off)
+    s1 = m9[:, :d]
+    mom = m9[:, 3:9]
     F = np.zeros((nbl, NFEAT), dtype=np.float64)
     boxes = np.arange(ls, le)
     F[:, 0] = lev
@@ -75,6 +72,27 @@ def level_features(fmm, lev, x_lev=None, off=None):
     F[:, 20] = np.log2(tree.get_box_npoints(boxes) + 1.0)
     F[:, 21] = (tree._coarse[boxes] >= 0).sum(1)
     return F.astype(np.float32)
+
+
+def box_moments(fmm, lev, x_lev, off):
+    """[nboxes_at_lev, 9] float64 from ``skf_box_moments``: mean offset of
+    each box's candidate points from its centre and their second central
+    moments (xx yy zz xy xz yz), in units of the box width."""
+    tree = fmm.tree
+    ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+    nbl = le - ls
+    dev = fmm.device
+    if x_lev is None:
+        ids_t = torch.from_numpy(np.ascontiguousarray(fmm._ids[lev], dtype=np.int64)).to(dev)
+        x_lev = fmm._XX_dev.index_select(0, ids_t)
+    x_lev = x_lev.contiguous()
+    off_t = torch.from_numpy(np.ascontiguousarray(off, dtype=np.int64)).to(dev)
+    cen = torch.from_numpy(np.ascontiguousarray(tree._box_center[ls:le], dtype=np.float64)).to(dev)
+    out = torch.empty((max(nbl, 1), 9), dtype=torch.float64, device=dev)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    _lib.check(_lib.load().skf_box_moments(nbl, tree.ndim, _lib.ptr(off_t), _lib.ptr(x_lev), _lib.ptr(cen),
+                                           float(tree.L0 * 0.5 ** lev), _lib.ptr(out), stream), "skf_box_moments")
+    return out[:nbl].cpu().numpy()
 
 
 def rank_target(rank, bs):
@@ -229,18 +247,65 @@ class RankMLP:
         return m
 
 
-class LearnedRankPredictor:
-    """Callable for ``RecursiveSkeletonization.rank_predictor``: the
-    predicted pivoted-QR rank of each box plus ``margin`` (the randomized ID
-    detects its rank with a stricter rule on the sketch, a few above the
-    pivoted-QR rank), capped at the box size.  It sets the first sketch size."""
+class CalibratedRankPredictor:
+    """Callable for ``RecursiveSkeletonization.rank_predictor`` that turns a
+    per-box estimate y of the rank target (``estimate``) into sketch ranks.
 
-    def __init__(self, model: RankMLP, margin=8):
-        self.model = model
+    The build runs from the finest level to the root, so the ranks of level
+    l + 1 are known when level l is predicted (kept randomized IDs report
+    their sketch rank, the others their pivoted-QR rank; boxes left at full
+    rank are not used).  Their error e =
+    actual - y is fitted as a + b y by least squares, and level l's estimate
+    becomes y + max(0, a + b y + q), q the ``calibrate`` quantile of the fit's
+    residuals: this follows an estimate that drifts, level by level and with
+    the box size, on a point distribution it was not fitted to.  The
+    predicted rank is then ``margin`` above the corrected estimate, capped at
+    the box size."""
+
+    def __init__(self, margin=10, calibrate=0.9):
         self.margin = int(margin)
+        self.calibrate = calibrate
+        self.shifts = {}
+        self._prev = None
+
+    def estimate(self, fmm, lev, boxes, x_lev, off):
+        raise NotImplementedError
+
+    def _correction(self, fmm, lev):
+        """(a, b, q) fitted on level lev + 1 of the same build, else None."""
+        p = self._prev
+        if not self.calibrate or p is None or p[0]() is not fmm or p[1] != lev + 1:
+            return None
+        _, _, boxes, y, bs = p
+        rank = fmm.rank_list[boxes]
+        keep = (bs > 0) & (rank < bs)  # full-rank boxes say nothing of the estimate
+        if np.count_nonzero(keep) < 2:
+            return None
+        yk = y[keep]
+        err = rank_target(rank[keep], bs[keep]) - yk
+        A = np.stack([np.ones_like(yk), yk], 1)
+        coef = np.linalg.lstsq(A, err, rcond=None)[0]
+        q = float(np.quantile(err - A @ coef, self.calibrate))
+        return float(coef[0]), float(coef[1]), q
 
     def __call__(self, fmm, lev, boxes, x_lev, off):
-        F = level_features(fmm, lev, x_lev, off)
         bs = np.diff(off)
-        k = rank_from_target(self.model.predict(F), bs) + self.margin
+        y = np.asarray(self.estimate(fmm, lev, boxes, x_lev, off), np.float64)
+        fit = self._correction(fmm, lev)
+        shift = np.zeros_like(y) if fit is None else np.maximum(fit[0] + fit[1] * y + fit[2], 0.0)
+        self.shifts[lev] = float(shift.mean()) if shift.size else 0.0
+        self._prev = (weakref.ref(fmm), lev, np.asarray(boxes), y, bs)
+        k = rank_from_target(y + shift, bs) + self.margin
         return np.clip(k, 1, np.maximum(bs, 1))
+
+
+class LearnedRankPredictor(CalibratedRankPredictor):
+    """The rank network's estimate (``RankMLP`` on ``level_features``),
+    calibrated level by level.  It sets the sketch size of every box."""
+
+    def __init__(self, model: RankMLP, margin=10, calibrate=0.9):
+        super().__init__(margin, calibrate)
+        self.model = model
+
+    def estimate(self, fmm, lev, boxes, x_lev, off):
+        return self.model.predict(level_features(fmm, lev, x_lev, off))

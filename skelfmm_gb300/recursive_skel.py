@@ -119,8 +119,8 @@ class RecursiveSkeletonization:
         self.oversample = 10   # sketch rows beyond the predicted rank
         self.rho = 16          # nonzeros per sketch row
         self.nchk = 16         # proxy rows of the residual check
-        self.sketch_factor = 0.25  # rank rule on the sketch: |R_kk| <= factor * tol * |R_00|
-        self.resid_factor = 1.0  # keep the randomized ID when residual <= factor * tol
+        self.sketch_factor = 0.5  # rank rule on the sketch: |R_kk| <= factor * tol * |R_00|
+        self.resid_factor = 2.0  # keep the randomized ID when its residual on checked rows <= factor * tol
         self.seed = 12345
         self._XX_dev = torch.from_numpy(np.ascontiguousarray(tree.XX)).to(self.device)
         self._geom_dev = None

@@ -77,6 +77,43 @@ def test_training_reduces_loss():
     assert np.mean((pred - y) ** 2) < 0.1 * np.var(y)
 
 
+@pytest.mark.parametrize("geo,ndim", [("cube", 3), ("gaussian_clusters", 3), ("square", 2)])
+def test_box_moments_match_numpy(geo, ndim):
+    """The feature kernel's per-box offsets and central moments against a
+    numpy restatement over the same candidate points."""
+    from skelfmm_gb300 import operators
+    from skelfmm_gb300.rank_model import box_moments
+    from skelfmm_gb300.recursive_skel import RecursiveSkeletonization
+    from skelfmm_gb300.tree import BalancedTree, get_point_dist
+
+    pts = get_point_dist(30000, geo, rng=np.random.default_rng(3))
+    tree = BalancedTree(pts, 64)
+    op = operators.LAPLACE_3D if ndim == 3 else operators.LAPLACE_2D
+    f = RecursiveSkeletonization(tree, op, 0.0, 1e-6)
+    f.skel_tree(500)
+    checked = 0
+    for lev in range(f.root_level + 1, tree.nlevels):
+        if f._ids[lev] is None:
+            continue
+        ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+        off = f._off[lev]
+        bs = np.diff(off)
+        w = float(tree.L0 * 0.5 ** lev)
+        seg = np.repeat(np.arange(le - ls), bs)
+        rel = np.zeros((seg.shape[0], 3))
+        rel[:, :ndim] = (tree.XX[f._ids[lev]] - tree._box_center[ls:le][seg]) / w
+        cnt = np.maximum(bs, 1).astype(np.float64)
+        s1 = np.stack([np.bincount(seg, weights=rel[:, i], minlength=le - ls) for i in range(3)], 1) / cnt[:, None]
+        want = np.zeros((le - ls, 9))
+        want[:, :3] = s1
+        for k, (i, j) in enumerate([(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]):
+            want[:, 3 + k] = np.bincount(seg, weights=rel[:, i] * rel[:, j], minlength=le - ls) / cnt - s1[:, i] * s1[:, j]
+        got = box_moments(f, lev, None, off)
+        assert np.allclose(got, want, rtol=1e-12, atol=1e-14)
+        checked += 1
+    assert checked > 0
+
+
 def _cube_build(rank_predictor=None, n=40000, leaf=64, seed=0):
     from skelfmm_gb300 import operators
     from skelfmm_gb300.plan import Plan
