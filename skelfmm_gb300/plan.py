@@ -148,6 +148,11 @@ def ragged_from_reference(tree, fmm, operator, kappa=0.0):
     )
 
 
+# translation kernel variants (operator, precision, symmetric, shape) that
+# have run in this process: their first launch carries the module load
+_WARMED = set()
+
+
 class Plan:
     """A built operator resident on the device (owns an ``skf_plan``)."""
 
@@ -249,8 +254,17 @@ class Plan:
         for sym, shape in cands:
             self.set_option(_lib.OPT_SYMMETRIC, sym)
             self.set_option(_lib.OPT_SYM_SHAPE if sym else _lib.OPT_PACKED_SHAPE, shape)
-            self.time_translations(precision, reps=1)
-            results[(sym, shape)] = self.time_translations(precision, reps=reps)
+            key = (int(self.op), int(precision), sym, shape)
+            ms = None
+            if key not in _WARMED:
+                # first launch of this kernel variant in the process (module load)
+                ms = self.time_translations(precision, reps=1)
+                _WARMED.add(key)
+            if ms is None or ms < 20.0:
+                # long launches are timed once: their spread is well below
+                # the differences between shapes
+                ms = self.time_translations(precision, reps=reps)
+            results[(sym, shape)] = ms
         best = min(results, key=results.get)
         self.set_option(_lib.OPT_SYMMETRIC, best[0])
         self.set_option(_lib.OPT_SYM_SHAPE if best[0] else _lib.OPT_PACKED_SHAPE, best[1])

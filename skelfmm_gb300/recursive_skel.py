@@ -113,6 +113,8 @@ class RecursiveSkeletonization:
         self.level_times = {}
         self.level_stats = {}
         self._resid_by_lev = {}
+        self._status_by_lev = {}  # per box: 0 pivoted QR, 10 * rounds + 1 kept, + 2 rejected
+        self._sketch_by_lev = {}  # per box: sketch rank tried (0: none)
         # optional callable(fmm, lev, boxes, x_lev, off) -> predicted ranks (int64,
         # -1 = no prediction): enables the sampled (randomized) IDs
         self.rank_predictor = None
@@ -263,6 +265,8 @@ class RecursiveSkeletonization:
             st = status.cpu().numpy()
             self._last_resid = resid.cpu().numpy()
             self._resid_by_lev[lev] = self._last_resid
+            self._status_by_lev[lev] = st
+            self._sketch_by_lev[lev] = kpred
             rounds = st // 10
             stats.update(randomized=int(np.count_nonzero(st > 0)), kept=int(np.count_nonzero(st % 10 == 1)),
                          fallback=int(np.count_nonzero(st % 10 == 2)), sketch_rounds=int(rounds.sum()),
@@ -418,13 +422,19 @@ class RecursiveSkeletonization:
         if verbose:
             print("\t root level %d, %d root boxes, %d entries" % (self.root_level, root_boxes.shape[0], off[-1]))
 
+    def _gather_xyz(self, pid):
+        """Coordinates of the points ``pid`` (host float64 [len, ndim]),
+        gathered from the build's device copy."""
+        idx = torch.from_numpy(np.ascontiguousarray(pid, dtype=np.int64)).to(self.device)
+        return self._XX_dev.index_select(0, idx).cpu().numpy()
+
     def ragged(self):
         geom = None if self.geometry is None else self.geometry[self.entry_pid]
         return RaggedBuild(
             op=self.op_id, ndim=self.ndim, kappa=self.kappa, npoints=int(self.N), nlevels=int(self.nlevels),
             root_level=int(self.root_level), box_level=self.tree.get_boxes_levels().astype(np.int32),
             box_off=self.box_off, box_rank=self.rank_list.astype(np.int32),
-            entry_xyz=np.ascontiguousarray(self.tree.XX[self.entry_pid]), entry_geom=geom,
+            entry_xyz=self._gather_xyz(self.entry_pid), entry_geom=geom,
             entry_pslot=self.entry_pslot, perm_entry=self.perm_entry, perm_point=self.perm_point,
             t_off=self.t_off, t_data=self.t_data, list_off=self.list_off, list_src=self.list_src,
             list_kind=self.list_kind,

@@ -114,13 +114,13 @@ def test_box_moments_match_numpy(geo, ndim):
     assert checked > 0
 
 
-def _cube_build(rank_predictor=None, n=40000, leaf=64, seed=0):
+def _cube_build(rank_predictor=None, n=100000, leaf=256, seed=0, geo="cube"):
     from skelfmm_gb300 import operators
     from skelfmm_gb300.plan import Plan
     from skelfmm_gb300.recursive_skel import RecursiveSkeletonization
-    from skelfmm_gb300.tree import BalancedTree
+    from skelfmm_gb300.tree import BalancedTree, get_point_dist
 
-    pts = np.random.default_rng(seed).random((n, 3))
+    pts = get_point_dist(n, geo, rng=np.random.default_rng(seed))
     tree = BalancedTree(pts, leaf)
     f = RecursiveSkeletonization(tree, operators.LAPLACE_3D, 0.0, 1e-6)
     f.rank_predictor = rank_predictor
@@ -195,11 +195,61 @@ def test_network_gains_over_build_without_it(reference_build):
             return np.full(boxes.shape[0], 8, dtype=np.int64)
 
     # boxes of ~200 points with ranks ~120: sketches are smaller than boxes
-    _, fl, _ = _cube_build(LearnedRankPredictor(RankMLP.load()), n=100000, leaf=256)
-    _, fn, _ = _cube_build(NoModel(), n=100000, leaf=256)
+    _, fl, _ = _cube_build(LearnedRankPredictor(RankMLP.load()))
+    _, fn, _ = _cube_build(NoModel())
     kept_l = sum(s["kept"] for s in fl.level_stats.values())
     kept_n = sum(s["kept"] for s in fn.level_stats.values())
     fb_l = sum(s["fallback"] for s in fl.level_stats.values())
     fb_n = sum(s["fallback"] for s in fn.level_stats.values())
     assert kept_l > 2 * kept_n
     assert fb_l < 0.5 * fb_n
+
+
+def _id_work(f):
+    """FP64 work model of a build's IDs: rows x n x min(rows, n) per box,
+    rows = the sketch for kept randomized IDs, the sketch plus the proxy
+    matrix for rejected ones, the proxy matrix otherwise."""
+    tree = f.tree
+    w = 0.0
+    for lev in range(f.root_level + 1, tree.nlevels):
+        if f._ids[lev] is None:
+            continue
+        n = np.diff(f._off[lev]).astype(np.float64)
+        m = float(f._mrows(lev))
+        full = m * n * np.minimum(m, n)
+        st = f._status_by_lev.get(lev)
+        if st is None:
+            w += full.sum()
+            continue
+        s = f._sketch_by_lev[lev].astype(np.float64) + f.oversample
+        sk = s * n * np.minimum(s, n)
+        w += np.where(st % 10 == 1, sk, np.where(st % 10 == 2, sk + full, full)).sum()
+    return w
+
+
+def test_network_gains_over_calibrated_constant():
+    """The same calibrated predictor with a constant estimate (the training
+    set's mean target for every box) in place of the network, on clustered
+    points (boxes of very different occupancy, a distribution the network
+    was not trained on): the network's per-box estimates keep several times
+    more randomized IDs and cut the modelled FP64 work of the IDs below
+    both the constant's and the pivoted-QR build's."""
+    from skelfmm_gb300.rank_model import CalibratedRankPredictor, LearnedRankPredictor, RankMLP
+
+    model = RankMLP.load()
+
+    class Const(CalibratedRankPredictor):
+        def estimate(self, fmm, lev, boxes, x_lev, off):
+            return np.full(len(boxes), model.y_mu)
+
+    kw = dict(n=200000, leaf=128, geo="gaussian_clusters")
+    _, ff, _ = _cube_build(**kw)
+    _, fl, _ = _cube_build(LearnedRankPredictor(model), **kw)
+    _, fc, _ = _cube_build(Const(), **kw)
+    wf, wl, wc = _id_work(ff), _id_work(fl), _id_work(fc)
+    kept_l = sum(s["kept"] for s in fl.level_stats.values())
+    kept_c = sum(s["kept"] for s in fc.level_stats.values())
+    fb_l = sum(s["fallback"] for s in fl.level_stats.values())
+    assert kept_l > 3 * kept_c, (kept_l, kept_c)
+    assert fb_l < 0.05 * kept_l, (fb_l, kept_l)
+    assert wl < 0.95 * wc and wl < 0.95 * wf, (wl, wc, wf)
