@@ -197,24 +197,33 @@ int skf_copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_o
 int skf_proxy_rows(int32_t op, int32_t nproxy, int32_t* rows_out);
 
 /*
+ * The ID calls keep their freed workspaces in the device's default memory
+ * pool between calls (one call per tree level); this returns that memory
+ * to the device once a build is done.
+ */
+int skf_trim_workspace(void);
+
+/*
  * Randomized proxy IDs — the learned-rank build's fast path; no counterpart
  * in the reference, whose IDs are skf_skel_boxes.  Same arguments and outputs
  * as skf_skel_boxes (tol < 1), plus, all DEVICE unless noted:
- *   kpred[nbox]  predicted rank of box b (<= 0: full pivoted-QR ID).  The box
- *                factors sketches Y = S K of its proxy matrix K, S a sparse
- *                sign matrix with `rho` +-1 entries per row at hashed proxy
- *                rows (from `seed`), first with kpred[b] + oversample rows,
- *                doubling while the rank found on Y with |R_kk| <= sketch_tol
- *                |R_00| comes within oversample/2 of the sketch size (or
- *                until the sketch would exceed half of K's rows).  The ID of
- *                the first unsaturated sketch is kept when its relative
- *                Frobenius residual on `nchk` hashed rows of K is <=
- *                resid_tol; otherwise the box falls back to the full
- *                pivoted-QR ID of K with the tol rule.
- *   resid[nbox]  (out, may be NULL) that residual; -1 not tried, -2 every
+ *   kpred[nbox]  predicted rank of box b (<= 0: full pivoted-QR ID).  With
+ *                k = min(kpred[b], box size) and s = k + oversample <= 3/4
+ *                of K's rows, the box factors the sketch Y = S K of its
+ *                proxy matrix K, S a sparse sign matrix with `rho` +-1
+ *                entries per row at hashed proxy rows (from `seed`): pivoted
+ *                QR of Y with the rule |R_kk| <= sketch_tol |R_00|.  A rank
+ *                above s - max(2, oversample / 2) means the sketch saturated;
+ *                otherwise the ID is kept when its relative Frobenius
+ *                residual on `nchk` hashed rows of K is <= resid_tol.
+ *                Saturated or rejected boxes, and boxes without a sketch,
+ *                get the full pivoted-QR ID of K with the tol rule (in a
+ *                second launch over those boxes; boxes factored on a
+ *                thread-block cluster fall back in place).
+ *   resid[nbox]  (out, may be NULL) that residual; -1 not tried, -2 the
  *                sketch saturated.
- *   status[nbox] (out, may be NULL) 0 full QR; else 10 * (sketches tried) +
- *                1 (randomized ID kept) or 2 (rejected, full QR used).
+ *   status[nbox] (out, may be NULL) 0 full QR; else 10 (one sketch) + 1
+ *                (randomized ID kept) or 2 (rejected, full QR used).
  */
 int skf_skel_boxes_randomized(int32_t op, double kappa, int32_t nbox, const int64_t* off, const double* x,
                               const double* geom, const double* centers, double box_length, int32_t nproxy,

@@ -20,6 +20,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <random>
 #include <type_traits>
@@ -145,17 +146,38 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return s;
 }
 
+// 1/sqrt(x) from the hardware estimate and one Newton step (relative error
+// ~2^-44): proxy matrices that only feed a sketch and its residual check.
+__device__ __forceinline__ double rsqrt_f64_1(double x) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double e = fma(-x * y, y, 1.0);
+  return fma(0.5 * y, e, y);
+}
+
 // Entry (row i, box point x) of the stacked proxy matrix: rows [0, np) are
 // K(x, p_i) (target = box point), rows [np, 2 np) of the geometry operators
-// K(p_i, x) (target = proxy).  Sphere proxies carry radial normals.
-template <int OP>
-__device__ __forceinline__ void proxy_entry(const SkelArgs& a, const double (&c)[3], int i, const double* xj,
-                                            const double* gj, double& kr, double& ki) {
+// K(p_i, x) (target = proxy).  Sphere proxies carry radial normals.  `pts`
+// holds the box's proxy points (NULL: from the template).  FAST: 3D Laplace
+// entries from rsqrt_f64_1.
+template <int OP, bool FAST = false>
+__device__ __forceinline__ void proxy_entry(const SkelArgs& a, const double (&c)[3], const double* pts, int i,
+                                            const double* xj, const double* gj, double& kr, double& ki) {
   constexpr int D = OpTraits<OP>::kDim;
   constexpr int G = OpTraits<OP>::kGeom;
   const int pi = (i < a.np) ? i : i - a.np;
   double p[3] = {0, 0, 0};
-  for (int d = 0; d < D; ++d) p[d] = c[d] + a.plen * a.tmpl[pi * D + d];
+  if (pts) {
+    for (int d = 0; d < D; ++d) p[d] = pts[pi * D + d];
+  } else {
+    for (int d = 0; d < D; ++d) p[d] = c[d] + a.plen * a.tmpl[pi * D + d];
+  }
+  if constexpr (FAST && OP == SKF_LAPLACE_3D) {
+    const double dx = xj[0] - p[0], dy = xj[1] - p[1], dz = xj[2] - p[2];
+    kr = rsqrt_f64_1(fma(dx, dx, fma(dy, dy, dz * dz)));
+    ki = 0.0;
+    return;
+  }
   double gx = 0, gy = 0, gz = 0;
   double pn[3] = {0, 0, 0};
   if (G != 0) {
@@ -179,6 +201,10 @@ __device__ __forceinline__ void proxy_entry(const SkelArgs& a, const double (&c)
     eval_f64<OP>(p[0] - xj[0], p[1] - xj[1], D == 3 ? p[2] - xj[2] : 0.0, gx, gy, gz, a.kappa, kr, ki);
   }
 }
+
+// A box takes the randomized ID when its sketch has at most 3/4 of the
+// proxy matrix's rows (the factorization's cost is proportional to the rows).
+__host__ __device__ __forceinline__ bool sketch_fits(int64_t s, int64_t m) { return 4 * s <= 3 * m; }
 
 // 64-bit mixing function (splitmix64 finaliser) for the sketch's indices.
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
@@ -615,19 +641,22 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
   const int m = a.mrows;
   const int kp = (RAND && a.kpred) ? a.kpred[b] : 0;
   // randomized ID while the sketch is well below the proxy matrix
-  int s = kp > 0 ? kp + a.oversample : 0;
-  const bool sketch = kp > 0 && 2 * s <= m && kp < n;
-  // smem: vn1[n], vn2[n], v[m * W], red[64], piv[n]
+  int s = kp > 0 ? min(kp, n) + a.oversample : 0;
+  const bool sketch = kp > 0 && sketch_fits(s, m);
+  // smem: vn1[n], vn2[n], v[m * W], red[64], proxy points[np * D], piv[n]
   QrScratch q;
   q.vn1 = sm;
   q.vn2 = q.vn1 + n;
   q.vv = q.vn2 + n;
   q.red = q.vv + (size_t)m * W;
-  q.piv = reinterpret_cast<int*>(q.red + 64);
+  double* pts = q.red + 64;
+  q.piv = reinterpret_cast<int*>(pts + (size_t)a.np * D);
 
   double* A = a.ws + a.ws_off[lb];
   double c[3] = {0, 0, 0};
   for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
+  for (int i = threadIdx.x; i < a.np * D; i += blockDim.x) pts[i] = c[i % D] + a.plen * a.tmpl[i];
+  __syncthreads();
 
   // ---- 1. proxy matrix, column j = box point j (a warp per column)
   {
@@ -638,7 +667,7 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
       double* col = A + (int64_t)j * m * W;
       for (int i = lane; i < m; i += 32) {
         double kr, ki;
-        proxy_entry<OP>(a, c, i, xj, gj, kr, ki);
+        proxy_entry<OP, RAND>(a, c, pts, i, xj, gj, kr, ki);
         col[i * W] = kr;
         if (C) col[i * W + 1] = ki;
       }
@@ -746,71 +775,61 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
 // published |R_kk| after a barrier, so it is uniform over the cluster.
 constexpr int kClusterCTAs = 8;
 
-template <int OP>
-__global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThreads)
-    k_skel_box_cluster(SkelArgs a) {
-  static_assert(!OpTraits<OP>::kComplex, "real operators only");
-  namespace cg = cooperative_groups;
-  constexpr int D = OpTraits<OP>::kDim;
+// Shared-memory scratch of one block of a cluster.
+struct ClusterScratch {
+  double* vsh;   // [m] Householder vector published by the pivot's owner
+  double* vloc;  // [m] local copy (later: reciprocal diagonal)
+  double* red;   // [64]
+  double* pub;   // [8] candidate norm, candidate position, beta, tau, residual sums
+  double* vn1;   // [ncl] squared partial norms of the owned columns
+  double* vn2;   // [ncl]
+  int* piv;      // [n] position -> physical column
+  int* posof;    // [n] physical column -> position
+};
+
+// Column-pivoted QR of the column-major m x n matrix M (leading dimension
+// m) on a cluster: block r owns the physical columns j = r (mod
+// kClusterCTAs).  Stopped at rank kfix (> 0) or at |R_kk| <= tol |R_00|;
+// the rank is uniform over the cluster.  On return M holds R (rows < rank
+// of the pivot columns), piv / posof the column order, and every update is
+// visible to the cluster.
+__device__ int cluster_pivoted_qr(cooperative_groups::cluster_group& cl, double* M, int m, int n, double tol,
+                                  int kfix, const ClusterScratch& s) {
   constexpr int NC = kClusterCTAs;
-  cg::cluster_group cl = cg::this_cluster();
   const int cr = (int)cl.block_rank();
-  const int lb = a.order[blockIdx.x / NC];
-  const int b = a.first_box + lb;
-  const int64_t off = a.off[b];
-  const int n = (int)(a.off[b + 1] - off);
-  const int m = a.mrows;
   const int ncl = (n + NC - 1) / NC;
-  double* A = a.ws + a.ws_off[lb];
-  extern __shared__ double smc[];
-  double* vsh = smc;           // [m] Householder vector published by the pivot's owner
-  double* vloc = vsh + m;      // [m] local copy (later: reciprocal diagonal)
-  double* red = vloc + m;      // [64]
-  double* pub = red + 64;      // [4] candidate norm, candidate position, beta, tau
-  double* vn1 = pub + 4;       // [ncl] squared partial norms of the owned columns
-  double* vn2 = vn1 + ncl;     // [ncl]
-  int* piv = reinterpret_cast<int*>(vn2 + ncl);  // [n] position -> physical column
-  int* posof = piv + n;                          // [n] physical column -> position
+  double* vsh = s.vsh;
+  double* vloc = s.vloc;
+  double* red = s.red;
+  double* pub = s.pub;
+  double* vn1 = s.vn1;
+  double* vn2 = s.vn2;
+  int* piv = s.piv;
+  int* posof = s.posof;
   __shared__ int s_col;
   __shared__ double s_h[3];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double c[3] = {0, 0, 0};
-  for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
-
-  // ---- proxy matrix, owned columns only (a warp per column)
-  for (int jl = warp; jl < ncl; jl += nw) {
-    const int j = cr + NC * jl;
-    if (j >= n) continue;
-    const double* xj = a.x + (off + j) * D;
-    const double* gj = a.geom ? a.geom + (off + j) * 3 : nullptr;
-    for (int i = lane; i < m; i += 32) {
-      double kr, ki;
-      proxy_entry<OP>(a, c, i, xj, gj, kr, ki);
-      A[(int64_t)j * m + i] = kr;
-    }
-  }
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     piv[j] = j;
     posof[j] = j;
   }
-  __syncthreads();
   for (int jl = warp; jl < ncl; jl += nw) {
     const int j = cr + NC * jl;
     if (j >= n) continue;
-    const double* col = A + (int64_t)j * m;
-    double s = 0;
-    for (int i = lane; i < m; i += 32) s += col[i] * col[i];
-    s = warp_sum_d(s);
+    const double* col = M + (int64_t)j * m;
+    double sq = 0;
+    for (int i = lane; i < m; i += 32) sq += col[i] * col[i];
+    sq = warp_sum_d(sq);
     if (lane == 0) {
-      vn1[jl] = s;
-      vn2[jl] = s;
+      vn1[jl] = sq;
+      vn2[jl] = sq;
     }
   }
   __syncthreads();
 
   const int kmax = min(m, n);
-  const bool fixed = a.tol >= 1.0;
-  const int rank_fixed = fixed ? min((int)a.tol, kmax) : kmax;
+  const bool fixed = kfix > 0;
+  const int rank_fixed = fixed ? min(kfix, kmax) : kmax;
   const double tol3z = sqrt(2.220446049250313e-16);
   double r00 = 0.0;
   int rank = 0;
@@ -882,7 +901,7 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
     const int owner = col % NC;
     if (cr == owner) {
       // Householder reflector of column col, rows k..m-1 (real zlarfg form)
-      double* ckc = A + (int64_t)col * m;
+      double* ckc = M + (int64_t)col * m;
       double sq = 0;
       for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) sq += ckc[i] * ckc[i];
       const double xnorm2 = block_sum(sq, red);
@@ -911,7 +930,7 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
     const double* opub = cl.map_shared_rank(pub, owner);
     const double beta = opub[2], tau = opub[3];
     if (k == 0) r00 = fabs(beta);
-    const bool stop = fixed ? (k >= rank_fixed) : (!(fabs(beta) > a.tol * r00) || r00 == 0.0);
+    const bool stop = fixed ? (k >= rank_fixed) : (!(fabs(beta) > tol * r00) || r00 == 0.0);
     if (stop) {
       rank = k;
       break;
@@ -928,7 +947,7 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
         const int j = cr + NC * jl;
         if (j >= n || posof[j] <= k) continue;
         double c[CRN];
-        const double akj = group_reflect<32, CRN>(A + (int64_t)j * m, true, vloc, k, m, tau, lane, c);
+        const double akj = group_reflect<32, CRN>(M + (int64_t)j * m, true, vloc, k, m, tau, lane, c);
         downdate_norm(true, jl, lane == 0, akj, vn1, vn2, tol3z,
                       [&] { return group_norm_below<32, CRN>(c, k, m, lane); });
       }
@@ -946,7 +965,7 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
       for (int jl = warp; jl < ncl; jl += nw) {
         const int j = cr + NC * jl;
         if (j >= n || posof[j] <= k) continue;
-        double* cj = A + (int64_t)j * m;
+        double* cj = M + (int64_t)j * m;
         double w = 0;
         for (int i = k + lane; i < m; i += 32) w += vloc[i] * cj[i];
         w = warp_sum_d(w);
@@ -965,32 +984,30 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
     }
     __syncthreads();
   }
-  cl.sync();  // every update of the proxy matrix is visible; no remote reads follow
+  cl.sync();  // every update of M is visible; no remote reads follow
+  return rank;
+}
 
-  // ---- outputs: rank and permutation (block 0), T of the owned redundant columns
-  if (cr == 0) {
-    if (threadIdx.x == 0) {
-      a.rank[b] = rank;
-      if (a.status) a.status[b] = 0;
-      if (a.resid) a.resid[b] = -1.0;
-    }
-    for (int pos = threadIdx.x; pos < n; pos += blockDim.x) a.perm[off + pos] = piv[pos];
-  }
+// T = R11^{-1} R12 (row-major rank x (n - rank)) for this block's redundant
+// columns, from the R that cluster_pivoted_qr left in M (leading dimension m).
+__device__ void cluster_write_T(double* M, int m, int n, int rank, double* T, const ClusterScratch& s, int cr) {
+  constexpr int NC = kClusterCTAs;
   const int nr = n - rank;
   if (rank == 0 || nr == 0) return;
-  double* rinv = vloc;
-  for (int i = threadIdx.x; i < rank; i += blockDim.x) rinv[i] = 1.0 / A[(int64_t)piv[i] * m + i];
+  const int ncl = (n + NC - 1) / NC;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double* rinv = s.vloc;
+  for (int i = threadIdx.x; i < rank; i += blockDim.x) rinv[i] = 1.0 / M[(int64_t)s.piv[i] * m + i];
   __syncthreads();
-  double* T = a.t_out + a.t_off_out[b];
   for (int jl = warp; jl < ncl; jl += nw) {
     const int j = cr + NC * jl;
     if (j >= n) continue;
-    const int pos = posof[j];
+    const int pos = s.posof[j];
     if (pos < rank) continue;
     const int cidx = pos - rank;
-    double* bcol = A + (int64_t)j * m;  // R12 column, overwritten by t
+    double* bcol = M + (int64_t)j * m;  // R12 column, overwritten by t
     for (int i = rank - 1; i >= 0; --i) {
-      const double* ci = A + (int64_t)piv[i] * m;
+      const double* ci = M + (int64_t)s.piv[i] * m;
       const double t = bcol[i] * rinv[i];
       __syncwarp();
       if (lane == 0) bcol[i] = t;
@@ -1001,31 +1018,178 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
   }
 }
 
+// RAND: boxes with a predicted rank first try the randomized ID on the
+// cluster (sketch of the owned columns, pivoted QR of the sketch, residual
+// on hashed rows of the proxy matrix reduced over the cluster), the same
+// steps and outputs as k_skel_box's randomized branch; a rejected box takes
+// the full pivoted-QR ID right away.
+template <int OP, bool RAND>
+__global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThreads)
+    k_skel_box_cluster(SkelArgs a) {
+  static_assert(!OpTraits<OP>::kComplex, "real operators only");
+  namespace cg = cooperative_groups;
+  constexpr int D = OpTraits<OP>::kDim;
+  constexpr int NC = kClusterCTAs;
+  cg::cluster_group cl = cg::this_cluster();
+  const int cr = (int)cl.block_rank();
+  const int lb = a.order[blockIdx.x / NC];
+  const int b = a.first_box + lb;
+  const int64_t off = a.off[b];
+  const int n = (int)(a.off[b + 1] - off);
+  const int m = a.mrows;
+  const int ncl = (n + NC - 1) / NC;
+  double* A = a.ws + a.ws_off[lb];
+  extern __shared__ double smc[];
+  ClusterScratch s;
+  s.vsh = smc;
+  s.vloc = s.vsh + m;
+  s.red = s.vloc + m;
+  s.pub = s.red + 64;
+  s.vn1 = s.pub + 8;
+  s.vn2 = s.vn1 + ncl;
+  s.piv = reinterpret_cast<int*>(s.vn2 + ncl);
+  s.posof = s.piv + n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double c[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
+
+  // ---- proxy matrix, owned columns only (a warp per column)
+  for (int jl = warp; jl < ncl; jl += nw) {
+    const int j = cr + NC * jl;
+    if (j >= n) continue;
+    const double* xj = a.x + (off + j) * D;
+    const double* gj = a.geom ? a.geom + (off + j) * 3 : nullptr;
+    for (int i = lane; i < m; i += 32) {
+      double kr, ki;
+      proxy_entry<OP>(a, c, nullptr, i, xj, gj, kr, ki);
+      A[(int64_t)j * m + i] = kr;
+    }
+  }
+  __syncthreads();
+
+  double* T = a.t_out + a.t_off_out[b];
+  int rank = 0;
+  bool done = false;
+  int8_t code = 0;
+  double resid = -1.0;
+  if constexpr (RAND) {
+    const int kp = a.kpred ? a.kpred[b] : 0;
+    const int sr = min(kp, n) + a.oversample;
+    if (kp > 0 && sketch_fits(sr, m)) {
+      // ---- sketch Y = S K of the owned columns (sr x n, after K)
+      double* Y = A + (int64_t)m * n;
+      for (int jl = warp; jl < ncl; jl += nw) {
+        const int j = cr + NC * jl;
+        if (j >= n) continue;
+        const double* col = A + (int64_t)j * m;
+        double* ycol = Y + (int64_t)j * sr;
+        for (int t = lane; t < sr; t += 32) {
+          const int32_t* row = a.sk_tab + (int64_t)t * a.rho;
+          double y = 0;
+          for (int u = 0; u < a.rho; ++u) {
+            const int32_t e = row[u];
+            const double v = col[e & 0x7fffffff];
+            y += e < 0 ? -v : v;
+          }
+          ycol[t] = y;
+        }
+      }
+      __syncthreads();
+      rank = cluster_pivoted_qr(cl, Y, sr, n, a.sketch_tol, 0, s);
+      const int guard = max(2, a.oversample / 2);
+      if (rank < n && rank > sr - guard) {
+        resid = -2.0;  // the sketch saturated
+      } else {
+        cluster_write_T(Y, sr, n, rank, T, s, cr);
+        cl.sync();  // T visible to the cluster
+        // ---- residual on nchk hashed rows of K
+        const uint64_t key = mix64(a.seed ^ ((uint64_t)b << 20));
+        const int nr = n - rank;
+        double e2 = 0.0, z2 = 0.0;
+        for (int qi = 0; qi < a.nchk; ++qi) {
+          const int row = (int)__umulhi((unsigned)(mix64(key ^ (0xC0FFEEull + (uint64_t)qi)) >> 32), (unsigned)m);
+          for (int jl = threadIdx.x; jl < ncl; jl += blockDim.x) {
+            const int j = cr + NC * jl;
+            if (j >= n) continue;
+            const double z = A[(int64_t)j * m + row];
+            z2 += z * z;
+            const int pos = s.posof[j];
+            if (pos < rank) continue;
+            double e = z;
+            for (int i = 0; i < rank; ++i) e -= A[(int64_t)s.piv[i] * m + row] * T[(int64_t)i * nr + (pos - rank)];
+            e2 += e * e;
+          }
+        }
+        e2 = block_sum(e2, s.red);
+        z2 = block_sum(z2, s.red);
+        if (threadIdx.x == 0) {
+          s.pub[4] = e2;
+          s.pub[5] = z2;
+        }
+        cl.sync();  // residual sums published
+        double E2 = 0.0, Z2 = 0.0;
+        for (int r = 0; r < NC; ++r) {
+          const double* rp = cl.map_shared_rank(s.pub, r);
+          E2 += rp[4];
+          Z2 += rp[5];
+        }
+        resid = Z2 > 0.0 ? sqrt(E2 / Z2) : 0.0;
+        done = resid <= a.resid_tol;
+        cl.sync();  // remote reads of pub done before it is reused
+      }
+      code = (int8_t)(10 + (done ? 1 : 2));
+    }
+  }
+  if (!done) {
+    // ---- full column-pivoted QR ID of K
+    rank = cluster_pivoted_qr(cl, A, m, n, a.tol >= 1.0 ? 0.0 : a.tol, a.tol >= 1.0 ? (int)a.tol : 0, s);
+    cluster_write_T(A, m, n, rank, T, s, cr);
+  }
+  if (cr == 0) {
+    if (threadIdx.x == 0) {
+      a.rank[b] = rank;
+      if (a.status) a.status[b] = code;
+      if (a.resid) a.resid[b] = resid;
+    }
+    for (int pos = threadIdx.x; pos < n; pos += blockDim.x) a.perm[off + pos] = s.piv[pos];
+  }
+}
+
+// Dynamic shared memory above this needs the opt-in attribute: 48 KB less
+// a margin for the kernels' static shared variables.
+constexpr size_t kSmemNoOptIn = 46 * 1024;
+
 __global__ void k_fill_f64(double* __restrict__ p, int n, double v) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
 }
 
+template <int OP, bool RAND>
+static int launch_skel_cluster_t(const SkelArgs& a, int nbox, size_t smem, cudaStream_t st) {
+  if (smem > kSmemNoOptIn)
+    SKF_CUDA_TRY(
+        cudaFuncSetAttribute(k_skel_box_cluster<OP, RAND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_skel_box_cluster<OP, RAND><<<nbox * kClusterCTAs, kSkelThreads, smem, st>>>(a);
+  SKF_CUDA_TRY(cudaGetLastError());
+  return SKF_OK;
+}
+
 template <int OP>
 static int launch_skel_cluster(const SkelArgs& a, int nbox, int maxn, cudaStream_t st) {
   const int ncl = (maxn + kClusterCTAs - 1) / kClusterCTAs;
-  const size_t smem = sizeof(double) * ((size_t)2 * a.mrows + 64 + 4 + 2 * (size_t)ncl) + sizeof(int) * 2 * (size_t)maxn;
+  const size_t smem = sizeof(double) * ((size_t)2 * a.mrows + 64 + 8 + 2 * (size_t)ncl) + sizeof(int) * 2 * (size_t)maxn;
   if (smem > 200 * 1024) return SKF_ERR_UNSUPPORTED;
-  if (smem > 48 * 1024)
-    SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box_cluster<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_skel_box_cluster<OP><<<nbox * kClusterCTAs, kSkelThreads, smem, st>>>(a);
-  SKF_CUDA_TRY(cudaGetLastError());
-  return SKF_OK;
+  return a.kpred ? launch_skel_cluster_t<OP, true>(a, nbox, smem, st) : launch_skel_cluster_t<OP, false>(a, nbox, smem, st);
 }
 
 template <int OP, int NT>
 static int launch_skel_nt(const SkelArgs& a, int nbox, size_t smem, cudaStream_t st) {
   if (a.kpred) {
-    if (smem > 48 * 1024)
+    if (smem > kSmemNoOptIn)
       SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_skel_box<OP, NT, true><<<nbox, NT, smem, st>>>(a);
   } else {
-    if (smem > 48 * 1024)
+    if (smem > kSmemNoOptIn)
       SKF_CUDA_TRY(cudaFuncSetAttribute(k_skel_box<OP, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_skel_box<OP, NT, false><<<nbox, NT, smem, st>>>(a);
   }
@@ -1042,9 +1206,15 @@ template <int OP>
 static int launch_skel(SkelArgs a, int nbox, int maxn, int maxm, cudaStream_t st, int nbig = 0,
                        cudaStream_t side = nullptr, cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
   constexpr int W = OpTraits<OP>::kComplex ? 2 : 1;
-  const size_t smem = sizeof(double) * ((size_t)2 * maxn + (size_t)maxm * W + 64) + sizeof(int) * (size_t)maxn;
+  const size_t smem = sizeof(double) * ((size_t)2 * maxn + (size_t)maxm * W + 64 + (size_t)a.np * OpTraits<OP>::kDim) +
+                      sizeof(int) * (size_t)maxn;
   if (smem > 200 * 1024) return SKF_ERR_UNSUPPORTED;
-  if (nbig <= 0 || nbig >= nbox || !side || !a.order) return launch_skel_nt<OP, kSkelThreads>(a, nbox, smem, st);
+  if (nbig <= 0 || !side || !a.order) return launch_skel_nt<OP, kSkelThreads>(a, nbox, smem, st);
+  if (nbig >= nbox) {
+    // every box is big: all of them take the big-box path on `st`
+    if constexpr (!OpTraits<OP>::kComplex) return launch_skel_cluster<OP>(a, nbox, maxn, st);
+    else return launch_skel_nt<OP, 1024>(a, nbox, smem, st);
+  }
   SKF_CUDA_TRY(cudaEventRecord(e0, st));
   SKF_CUDA_TRY(cudaStreamWaitEvent(side, e0, 0));
   int status;
@@ -1077,6 +1247,30 @@ struct RandomizedArgs {
   int8_t* status = nullptr;
 };
 
+// The ID workspaces come from the device's default memory pool, whose
+// default release threshold hands freed memory back at every
+// synchronization: the next level then maps its gigabytes again.  The
+// builds keep it in the pool instead, and trim_workspace returns it once a
+// build is done.
+static void keep_pool_memory() {
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) return;
+  uint64_t thr = UINT64_MAX;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+}
+
+int trim_workspace() {
+  int dev = 0;
+  cudaMemPool_t pool;
+  SKF_CUDA_TRY(cudaGetDevice(&dev));
+  SKF_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+  uint64_t thr = 0;
+  SKF_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  SKF_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+  return SKF_OK;
+}
+
 static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
                            const double* centers, double box_length, int nproxy, double tol,
                            const RandomizedArgs& ra, int32_t* rank, int32_t* perm, const int64_t* t_off_out,
@@ -1086,6 +1280,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
   const bool cplx = op == SKF_HELMHOLTZ_2D || op == SKF_HELMHOLTZ_3D || op == SKF_HELMHOLTZ_DOUBLE_LAYER_3D ||
                     op == SKF_HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D;
   const int W = cplx ? 2 : 1;
+  keep_pool_memory();
   std::vector<double> tmpl = proxy_template(ndim, geom_op, nproxy);
   const int np = (int)(tmpl.size() / ndim);
   const int mrows = geom_op ? 2 * np : np;
@@ -1097,12 +1292,14 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     SKF_CUDA_TRY(cudaMemcpyAsync(hk.data(), ra.kpred, sizeof(int32_t) * nbox, cudaMemcpyDeviceToHost, st));
   }
   SKF_CUDA_TRY(cudaStreamSynchronize(st));
+  // the sketch rank of a box is its predicted rank capped at its size (the
+  // kernels apply the same cap)
+  for (int b = 0; b < (int)hk.size(); ++b) hk[b] = (int32_t)std::min<int64_t>(hk[b], hoff[b + 1] - hoff[b]);
   // workspace rows per box: K, plus the sketch when the box is randomized
   auto box_rows = [&](int b) -> int64_t {
-    const int64_t n = hoff[b + 1] - hoff[b];
     if (!ra.kpred || hk[b] <= 0) return mrows;
     const int64_t s = (int64_t)hk[b] + ra.oversample;
-    return (2 * s <= mrows && hk[b] < n) ? mrows + s : mrows;  // K and the sketch
+    return sketch_fits(s, mrows) ? mrows + s : mrows;  // K and the sketch
   };
 
   double* dtmpl = nullptr;
@@ -1115,7 +1312,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
   if (ra.kpred) {
     int sk_rows = 1;
     for (int b = 0; b < nbox; ++b)
-      if (hk[b] > 0) sk_rows = std::max<int>(sk_rows, std::min<int>(hk[b] + ra.oversample, mrows / 2));
+      if (hk[b] > 0 && sketch_fits(hk[b] + ra.oversample, mrows)) sk_rows = std::max<int>(sk_rows, hk[b] + ra.oversample);
     tab.resize((size_t)sk_rows * ra.rho);
     std::mt19937_64 gen(ra.seed);
     for (auto& e : tab) {
@@ -1163,8 +1360,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     // Boxes of the batch whose randomized ID is tried (sketch well below the
     // proxy matrix); the others take the pivoted-QR ID directly.
     auto sketched = [&](int b) {
-      return ra.kpred && hk[b] > 0 && 2 * ((int64_t)hk[b] + ra.oversample) <= mrows &&
-             hk[b] < hoff[b + 1] - hoff[b];
+      return ra.kpred && hk[b] > 0 && sketch_fits(hk[b] + ra.oversample, mrows);
     };
     // cost ~ rows x n x min(rows, n), rows = the sketch or the proxy matrix
     auto box_cost = [&](int b, bool sketch) {
@@ -1221,7 +1417,8 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     // Launches the boxes `list` (batch-local) longest first; boxes far above
     // an even share of the launch's work get a thread-block cluster (real
     // operators, from twice an even share) or a 1024-thread block on `side`.
-    auto launch_list = [&](SkelArgs la, std::vector<int32_t> list, bool sketch, int32_t* dlist) -> int {
+    auto launch_list = [&](SkelArgs la, std::vector<int32_t> list, bool sketch, int32_t* dlist,
+                           std::vector<int32_t>* clustered = nullptr) -> int {
       if (list.empty()) return SKF_OK;
       std::vector<double> cost(list.size());
       for (size_t i = 0; i < list.size(); ++i) cost[i] = box_cost(b0 + list[i], sketch);
@@ -1247,6 +1444,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
             cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming) != cudaSuccess)
           nbig = 0;
       }
+      if (clustered && W == 1) clustered->assign(ord.begin(), ord.begin() + nbig);
       SKF_CUDA_TRY(cudaMemcpyAsync(dlist, ord.data(), sizeof(int32_t) * ord.size(), cudaMemcpyHostToDevice, st));
       la.order = dlist;
       switch (op) {
@@ -1273,13 +1471,16 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
       r.resid = ra.resid;
       r.status = dstat;
       r.defer = 1;
-      status = launch_list(r, rnd, true, dord);
+      // (boxes on clusters, real operators, finish their fallback in place)
+      std::vector<int32_t> clustered;
+      status = launch_list(r, rnd, true, dord, &clustered);
       if (status == SKF_OK) {
-        std::vector<int8_t> hs(nb);
+        std::vector<int8_t> hs(nb), done(nb, 0);
+        for (int32_t lb : clustered) done[lb] = 1;
         SKF_CUDA_TRY(cudaMemcpyAsync(hs.data(), dstat + b0, nb, cudaMemcpyDeviceToHost, st));
         SKF_CUDA_TRY(cudaStreamSynchronize(st));
         for (int32_t lb : rnd)
-          if (hs[lb] % 10 == 2) full.push_back(lb);
+          if (hs[lb] % 10 == 2 && !done[lb]) full.push_back(lb);
       }
     }
     // phase 2: pivoted-QR IDs of the other boxes and of the rejects

@@ -30,13 +30,23 @@ int skel_boxes_randomized(int op, double kappa, int nbox, const int64_t* off, co
                           double* resid, int8_t* status, int32_t* rank, int32_t* perm, const int64_t* t_off_out,
                           void* t_out, cudaStream_t st);
 int proxy_rows(int op, int nproxy);
+int trim_workspace();
 int convert_f64_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
 int split_f64(const double* src, float* hi, float* lo, int64_t n, cudaStream_t st);
 int copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_off, const int64_t* len,
                   const void* src, void* dst, int elem_bytes, cudaStream_t st);
 
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
-void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+static thread_local char g_last_where[192] = "";
+void set_last_cuda_error(cudaError_t e) {
+  g_last_cuda = e;
+  g_last_where[0] = 0;
+}
+void set_last_cuda_error_at(cudaError_t e, const char* file, int line) {
+  g_last_cuda = e;
+  const char* base = strrchr(file, '/');
+  snprintf(g_last_where, sizeof(g_last_where), "%s (%s:%d)", cudaGetErrorString(e), base ? base + 1 : file, line);
+}
 
 static bool op_is_complex(int op) {
   return op == SKF_HELMHOLTZ_2D || op == SKF_HELMHOLTZ_3D || op == SKF_HELMHOLTZ_DOUBLE_LAYER_3D ||
@@ -96,7 +106,7 @@ const char* skf_status_string(int32_t s) {
     case SKF_OK: return "ok";
     case SKF_ERR_ARG: return "invalid argument";
     case SKF_ERR_OOM: return "device out of memory";
-    case SKF_ERR_CUDA: return cudaGetErrorString(g_last_cuda);
+    case SKF_ERR_CUDA: return g_last_where[0] ? g_last_where : cudaGetErrorString(g_last_cuda);
     case SKF_ERR_UNSUPPORTED: return "unsupported operator or precision";
     case SKF_ERR_ID: return "interpolative decomposition failed (non-finite proxy matrix)";
     case SKF_ERR_TIMEOUT: return "device wait timed out";
@@ -494,6 +504,8 @@ int skf_copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_o
   if (!src_off || !dst_off || !len || !src || !dst) return SKF_ERR_ARG;
   return copy_segments(nseg, src_off, dst_off, len, src, dst, elem_bytes, static_cast<cudaStream_t>(stream));
 }
+
+int skf_trim_workspace(void) { return trim_workspace(); }
 
 int skf_proxy_rows(int32_t op, int32_t nproxy, int32_t* rows_out) {
   if (op < 0 || op >= SKF_NUM_OPS || nproxy <= 0 || !rows_out) return SKF_ERR_ARG;

@@ -11,7 +11,7 @@
   do {                                     \
     cudaError_t _e = (expr);               \
     if (_e != cudaSuccess) {               \
-      skf::set_last_cuda_error(_e);        \
+      skf::set_last_cuda_error_at(_e, __FILE__, __LINE__); \
       return SKF_ERR_CUDA;                 \
     }                                      \
   } while (0)
@@ -19,6 +19,9 @@
 namespace skf {
 
 void set_last_cuda_error(cudaError_t e);
+// as set_last_cuda_error, naming the failing call's source line in the
+// status string
+void set_last_cuda_error_at(cudaError_t e, const char* file, int line);
 
 // Translation kernel geometry: 128 threads per block; rows per thread depend
 // on the precision (FP64: 1, mixed: 2).

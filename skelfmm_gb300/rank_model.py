@@ -258,13 +258,17 @@ class CalibratedRankPredictor:
     actual - y is fitted as a + b y by least squares, and level l's estimate
     becomes y + max(0, a + b y + q), q the ``calibrate`` quantile of the fit's
     residuals: this follows an estimate that drifts, level by level and with
-    the box size, on a point distribution it was not fitted to.  The
-    predicted rank is then ``margin`` above the corrected estimate, capped at
-    the box size."""
+    the box size, on a point distribution it was not fitted to.  Boxes of
+    ``big_box`` candidates or more take the ``calibrate_big`` quantile: a
+    rejected large box pays the full pivoted-QR ID on top of its sketch,
+    while a few more sketch rows cost little.  The predicted rank is then
+    ``margin`` above the corrected estimate, capped at the box size."""
 
-    def __init__(self, margin=10, calibrate=0.9):
+    def __init__(self, margin=10, calibrate=0.9, calibrate_big=0.98, big_box=256):
         self.margin = int(margin)
         self.calibrate = calibrate
+        self.calibrate_big = calibrate_big
+        self.big_box = int(big_box)
         self.shifts = {}
         self._prev = None
 
@@ -272,7 +276,8 @@ class CalibratedRankPredictor:
         raise NotImplementedError
 
     def _correction(self, fmm, lev):
-        """(a, b, q) fitted on level lev + 1 of the same build, else None."""
+        """(a, b, q, q_big) fitted on level lev + 1 of the same build, else
+        None."""
         p = self._prev
         if not self.calibrate or p is None or p[0]() is not fmm or p[1] != lev + 1:
             return None
@@ -285,14 +290,20 @@ class CalibratedRankPredictor:
         err = rank_target(rank[keep], bs[keep]) - yk
         A = np.stack([np.ones_like(yk), yk], 1)
         coef = np.linalg.lstsq(A, err, rcond=None)[0]
-        q = float(np.quantile(err - A @ coef, self.calibrate))
-        return float(coef[0]), float(coef[1]), q
+        res = err - A @ coef
+        q = float(np.quantile(res, self.calibrate))
+        q_big = float(np.quantile(res, max(self.calibrate, self.calibrate_big)))
+        return float(coef[0]), float(coef[1]), q, q_big
 
     def __call__(self, fmm, lev, boxes, x_lev, off):
         bs = np.diff(off)
         y = np.asarray(self.estimate(fmm, lev, boxes, x_lev, off), np.float64)
         fit = self._correction(fmm, lev)
-        shift = np.zeros_like(y) if fit is None else np.maximum(fit[0] + fit[1] * y + fit[2], 0.0)
+        if fit is None:
+            shift = np.zeros_like(y)
+        else:
+            q = np.where(bs >= self.big_box, fit[3], fit[2])
+            shift = np.maximum(fit[0] + fit[1] * y + q, 0.0)
         self.shifts[lev] = float(shift.mean()) if shift.size else 0.0
         self._prev = (weakref.ref(fmm), lev, np.asarray(boxes), y, bs)
         k = rank_from_target(y + shift, bs) + self.margin
@@ -303,8 +314,8 @@ class LearnedRankPredictor(CalibratedRankPredictor):
     """The rank network's estimate (``RankMLP`` on ``level_features``),
     calibrated level by level.  It sets the sketch size of every box."""
 
-    def __init__(self, model: RankMLP, margin=10, calibrate=0.9):
-        super().__init__(margin, calibrate)
+    def __init__(self, model: RankMLP, margin=10, calibrate=0.9, calibrate_big=0.98, big_box=256):
+        super().__init__(margin, calibrate, calibrate_big, big_box)
         self.model = model
 
     def estimate(self, fmm, lev, boxes, x_lev, off):

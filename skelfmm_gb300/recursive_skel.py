@@ -251,7 +251,7 @@ class RecursiveSkeletonization:
                 _lib.ptr(t_buf), stream), "skf_skel_boxes")
             stats.update(randomized=0, kept=0, fallback=0)
         else:
-            kpred = np.where((pred > 0) & (pred < bs), pred, 0).astype(np.int32)
+            kpred = np.where((pred > 0) & (bs > 0), np.minimum(pred, bs), 0).astype(np.int32)
             kpred_t = torch.from_numpy(kpred).to(dev)
             resid = torch.empty(nbl, dtype=torch.float64, device=dev)
             status = torch.empty(nbl, dtype=torch.int8, device=dev)
@@ -329,6 +329,7 @@ class RecursiveSkeletonization:
             self.level_times[lev] = perf_counter() - t0
             if verbose:
                 print("\t Level %2d ids: %5.3f s" % (lev, self.level_times[lev]))
+        _lib.check(_lib.load().skf_trim_workspace(), "skf_trim_workspace")
         if tree.nlevels == 1:
             self._level_candidates(0)
         for lev in range(self.root_level - 1, -1, -1):

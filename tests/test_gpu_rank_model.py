@@ -231,9 +231,10 @@ def test_network_gains_over_calibrated_constant():
     """The same calibrated predictor with a constant estimate (the training
     set's mean target for every box) in place of the network, on clustered
     points (boxes of very different occupancy, a distribution the network
-    was not trained on): the network's per-box estimates keep several times
-    more randomized IDs and cut the modelled FP64 work of the IDs below
-    both the constant's and the pivoted-QR build's."""
+    was not trained on): both keep nearly every randomized ID, but the
+    constant's sketches are sized for the worst boxes of a level, so the
+    network's per-box estimates cut the modelled FP64 work of the IDs well
+    below the constant's and the pivoted-QR build's."""
     from skelfmm_gb300.rank_model import CalibratedRankPredictor, LearnedRankPredictor, RankMLP
 
     model = RankMLP.load()
@@ -248,8 +249,6 @@ def test_network_gains_over_calibrated_constant():
     _, fc, _ = _cube_build(Const(), **kw)
     wf, wl, wc = _id_work(ff), _id_work(fl), _id_work(fc)
     kept_l = sum(s["kept"] for s in fl.level_stats.values())
-    kept_c = sum(s["kept"] for s in fc.level_stats.values())
     fb_l = sum(s["fallback"] for s in fl.level_stats.values())
-    assert kept_l > 3 * kept_c, (kept_l, kept_c)
-    assert fb_l < 0.05 * kept_l, (fb_l, kept_l)
-    assert wl < 0.95 * wc and wl < 0.95 * wf, (wl, wc, wf)
+    assert fb_l < 0.02 * kept_l, (fb_l, kept_l)
+    assert wl < 0.6 * wc and wl < 0.4 * wf, (wl, wc, wf)
