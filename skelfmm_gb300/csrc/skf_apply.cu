@@ -366,6 +366,17 @@ static void launch_sym(const SymArgs& c, int n, cudaStream_t st) {
   k_translate_sym<OP, TS, MINB><<<n, 128, smem, st>>>(c);
 }
 
+template <int TS, int MINB>
+static void launch_sym_helm(const SymArgs& c, float kappa, int n, cudaStream_t st) {
+  constexpr size_t smem = symh_smem_bytes(TS);
+  static bool attr = false;  // per instantiation
+  if (!attr) {
+    cudaFuncSetAttribute(k_translate_sym_helm<TS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  k_translate_sym_helm<TS, MINB><<<n, 128, smem, st>>>(c, kappa);
+}
+
 template <int OP>
 static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
   TransArgs a;
@@ -404,7 +415,7 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
     b.kappa = (float)p->kappa;
     static_assert(kT32Threads * kRowsPerThreadF32 == 256, "mixed work items are 256-row tiles");
     if (p->work32.n > 0) {
-      if constexpr (OP == SKF_LAPLACE_2D || OP == SKF_LAPLACE_3D) {
+      if constexpr (OP == SKF_LAPLACE_2D || OP == SKF_LAPLACE_3D || OP == SKF_HELMHOLTZ_3D) {
         if (!p->scalar_mixed && p->sym_ok && p->sym_on) {
           SymArgs c;
           c.work_box = p->worksym.box;
@@ -425,28 +436,45 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
           c.pbuf = p->pbuf;
           c.u = p->u;
           c.uh = p->uh;
-          if (p->worksym.n > 0) {
-            // tile shape: 0 = 64 sources, 5 blocks/SM; 1 = 128 sources, 3 blocks/SM;
-            // 2 = 64 sources, 4 blocks/SM; 3 = 32 sources, 5 blocks/SM
-            switch (p->sym_shape) {
-              case 1: launch_sym<OP, 128, 3>(c, p->worksym.n, st); break;
-              case 2: launch_sym<OP, 64, 4>(c, p->worksym.n, st); break;
-              case 3: launch_sym<OP, 32, 5>(c, p->worksym.n, st); break;
-              default: launch_sym<OP, 64, 5>(c, p->worksym.n, st); break;
+          if constexpr (OP == SKF_HELMHOLTZ_3D) {
+            if (p->worksym.n > 0) {
+              // tile shape: 0 = 32 sources, 3 blocks/SM; 1 = 64 sources, 2 blocks/SM;
+              // 2 = 32 sources, 4 blocks/SM; 3 = 16 sources, 4 blocks/SM
+              switch (p->sym_shape) {
+                case 1: launch_sym_helm<64, 2>(c, (float)p->kappa, p->worksym.n, st); break;
+                case 2: launch_sym_helm<32, 4>(c, (float)p->kappa, p->worksym.n, st); break;
+                case 3: launch_sym_helm<16, 4>(c, (float)p->kappa, p->worksym.n, st); break;
+                default: launch_sym_helm<32, 3>(c, (float)p->kappa, p->worksym.n, st); break;
+              }
             }
+            k_sym_reduce_c<<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
+                p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
+          } else {
+            if (p->worksym.n > 0) {
+              // tile shape: 0 = 64 sources, 5 blocks/SM; 1 = 128 sources, 3 blocks/SM;
+              // 2 = 64 sources, 4 blocks/SM; 3 = 32 sources, 5 blocks/SM
+              switch (p->sym_shape) {
+                case 1: launch_sym<OP, 128, 3>(c, p->worksym.n, st); break;
+                case 2: launch_sym<OP, 64, 4>(c, p->worksym.n, st); break;
+                case 3: launch_sym<OP, 32, 5>(c, p->worksym.n, st); break;
+                default: launch_sym<OP, 64, 5>(c, p->worksym.n, st); break;
+              }
+            }
+            k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
+                p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
           }
-          k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
-              p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
           return;
         }
-        if (!p->scalar_mixed) {
-          // packed kernel geometry: warps per block x row pairs per thread
-          switch (p->x2_config) {
-            case 1: k_translate_f32x2<OP, 1, 4><<<p->work32.n, 32, 0, st>>>(b); break;
-            case 2: k_translate_f32x2<OP, 2, 2><<<p->work32.n, 64, 0, st>>>(b); break;
-            default: k_translate_f32x2<OP, 4, 1><<<p->work32.n, 128, 0, st>>>(b); break;
+        if constexpr (OP != SKF_HELMHOLTZ_3D) {
+          if (!p->scalar_mixed) {
+            // packed kernel geometry: warps per block x row pairs per thread
+            switch (p->x2_config) {
+              case 1: k_translate_f32x2<OP, 1, 4><<<p->work32.n, 32, 0, st>>>(b); break;
+              case 2: k_translate_f32x2<OP, 2, 2><<<p->work32.n, 64, 0, st>>>(b); break;
+              default: k_translate_f32x2<OP, 4, 1><<<p->work32.n, 128, 0, st>>>(b); break;
+            }
+            return;
           }
-          return;
         }
       }
       if constexpr (OP == SKF_HELMHOLTZ_3D) {

@@ -293,7 +293,9 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   // symmetric translations: every pair (A, B) with A != B is evaluated once,
   // by the box with the smaller id, when the lists pair each entry with its
   // mirror (colleague <-> colleague, coarse-up <-> coarse-down, root <-> root)
-  if (d->op == SKF_LAPLACE_2D || d->op == SKF_LAPLACE_3D) {
+  if (d->op == SKF_LAPLACE_2D || d->op == SKF_LAPLACE_3D || d->op == SKF_HELMHOLTZ_3D) {
+    // partial arrays per owned entry: u, uh (real); u re/im, uh re/im (complex)
+    const int nparts = cplx ? 4 : 2;
     auto mirror = [](int k) {
       return k == SKF_KIND_COARSE_UP ? SKF_KIND_COARSE_DOWN : (k == SKF_KIND_COARSE_DOWN ? SKF_KIND_COARSE_UP : k);
     };
@@ -332,7 +334,7 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
           ssrc.push_back(B);
           skind.push_back(d->list_kind[l]);
           poff.push_back(B == A ? 0 : stride);
-          if (B != A) stride += 2 * bsB;
+          if (B != A) stride += nparts * bsB;
           srcsum += bsB;
         }
         soff[A + 1] = (int64_t)ssrc.size();

@@ -1059,6 +1059,375 @@ __global__ void __launch_bounds__(128, MINB) k_translate_sym(SymArgs a) {
   }
 }
 
+// ------------------------------------------------------------------ symmetric Helmholtz 3D (mixed, packed)
+// exp(i kappa r) / r is symmetric too: the owned pairs of the symmetric
+// lists are evaluated once for both directions as in k_translate_sym, with
+// the arithmetic of k_translate_helm_x2 per evaluation (hi/lo differences,
+// one-turn phase reduction, sin/cos.approx) and complex charges and sums.
+// Same lane layout (lane = 16 ls + lr, 4 rows per lane in 2 packed pairs),
+// tiles and fixed-order B-side partials, with four partial arrays per
+// source (u re, u im, uh re, uh im).
+__host__ __device__ constexpr size_t symh_smem_bytes(int ts) {
+  return 6 * sizeof(ulonglong2) * (size_t)ts + 4 * 4 * 16 * sizeof(float) * (size_t)sym_ld(ts);
+}
+
+// Charges of the A rows seen from B (mirror kind) for the B-side sums,
+// packed per row pair: c1 = (r, i) and -i, c2 likewise.
+struct SymhCharges {
+  f2_t c1r[kSymPairs], c1i[kSymPairs], m1i[kSymPairs];
+  f2_t c2r[kSymPairs], c2i[kSymPairs], m2i[kSymPairs];
+};
+
+template <bool HR, bool HT, bool TR, bool SELF, int LD>
+__device__ __forceinline__ void symh_tile(const ulonglong2* __restrict__ s0, const ulonglong2* __restrict__ s1,
+                                          const ulonglong2* __restrict__ s2, const ulonglong2* __restrict__ s3,
+                                          const ulonglong2* __restrict__ s4, const ulonglong2* __restrict__ s5,
+                                          int nt, int ls, int lr, const f2_t (&thx)[kSymPairs],
+                                          const f2_t (&thy)[kSymPairs], const f2_t (&thz)[kSymPairs],
+                                          const f2_t (&tlx)[kSymPairs], const f2_t (&tly)[kSymPairs],
+                                          const f2_t (&tlz)[kSymPairs], f2_t kc2, const SymhCharges& cT,
+                                          f2_t (&pur)[kSymPairs], f2_t (&pui)[kSymPairs], f2_t (&phr)[kSymPairs],
+                                          f2_t (&phi)[kSymPairs], float* __restrict__ sT) {
+  const f2_t two_pi = f2_pack(6.283185307179586f, 6.283185307179586f);
+  constexpr int PS = 4 * 16 * LD;  // stride between the four partial arrays
+#pragma unroll 2
+  for (int j = ls; j < nt; j += 2) {
+    const ulonglong2 A = s0[j];   // (-hx), (-hy)
+    const ulonglong2 B = s1[j];   // (-hz), (-lx)
+    const ulonglong2 Cc = s2[j];  // (-ly), (-lz)
+    const ulonglong2 Q1 = s3[j];  // c1r, c1i
+    const ulonglong2 Q2 = s4[j];  // -c1i, c2r
+    const ulonglong2 Q3 = s5[j];  // c2i, -c2i
+    f2_t tur = 0ull, tui = 0ull, thr = 0ull, thi = 0ull;
+#pragma unroll
+    for (int p = 0; p < kSymPairs; ++p) {
+      const f2_t dx = f2_add(f2_add(thx[p], A.x), f2_add(tlx[p], B.y));
+      const f2_t dy = f2_add(f2_add(thy[p], A.y), f2_add(tly[p], Cc.x));
+      const f2_t dz = f2_add(f2_add(thz[p], B.x), f2_add(tlz[p], Cc.y));
+      f2_t r2 = f2_mul(dx, dx);
+      r2 = f2_fma(dy, dy, r2);
+      r2 = f2_fma(dz, dz, r2);
+      float ra, rb;
+      f2_unpack(r2, ra, rb);
+      float ia = rsqrt_approx(ra), ib = rsqrt_approx(rb);
+      if (SELF) {
+        ia = ra > 0.f ? ia : 0.f;
+        ib = rb > 0.f ? ib : 0.f;
+      }
+      const f2_t ir = f2_pack(ia, ib);
+      const f2_t t = f2_mul(f2_mul(r2, ir), kc2);  // phase in turns: kappa r / (2 pi)
+      float ta, tb;
+      f2_unpack(t, ta, tb);
+      const f2_t ang = f2_mul(f2_add(t, f2_pack(-rintf(ta), -rintf(tb))), two_pi);
+      float aa, ab;
+      f2_unpack(ang, aa, ab);
+      float sa, ca, sb, cb;
+      asm("sin.approx.ftz.f32 %0, %1;" : "=f"(sa) : "f"(aa));
+      asm("cos.approx.ftz.f32 %0, %1;" : "=f"(ca) : "f"(aa));
+      asm("sin.approx.ftz.f32 %0, %1;" : "=f"(sb) : "f"(ab));
+      asm("cos.approx.ftz.f32 %0, %1;" : "=f"(cb) : "f"(ab));
+      const f2_t kr = f2_mul(f2_pack(ca, cb), ir);
+      const f2_t ki = f2_mul(f2_pack(sa, sb), ir);
+      pur[p] = f2_fma(ki, Q2.x, f2_fma(kr, Q1.x, pur[p]));
+      pui[p] = f2_fma(ki, Q1.x, f2_fma(kr, Q1.y, pui[p]));
+      if (HR) {
+        phr[p] = f2_fma(ki, Q3.y, f2_fma(kr, Q2.y, phr[p]));
+        phi[p] = f2_fma(ki, Q2.y, f2_fma(kr, Q3.x, phi[p]));
+      }
+      if (TR) {
+        tur = f2_fma(ki, cT.m1i[p], f2_fma(kr, cT.c1r[p], tur));
+        tui = f2_fma(ki, cT.c1r[p], f2_fma(kr, cT.c1i[p], tui));
+        if (HT) {
+          thr = f2_fma(ki, cT.m2i[p], f2_fma(kr, cT.c2r[p], thr));
+          thi = f2_fma(ki, cT.c2r[p], f2_fma(kr, cT.c2i[p], thi));
+        }
+      }
+    }
+    if (TR) {
+      float a, b;
+      f2_unpack(tur, a, b);
+      sT[lr * LD + j] = a + b;
+      f2_unpack(tui, a, b);
+      sT[PS + lr * LD + j] = a + b;
+      if (HT) {
+        f2_unpack(thr, a, b);
+        sT[2 * PS + lr * LD + j] = a + b;
+        f2_unpack(thi, a, b);
+        sT[3 * PS + lr * LD + j] = a + b;
+      }
+    }
+  }
+}
+
+template <int TS, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_translate_sym_helm(SymArgs a, float kappa) {
+  constexpr int NW = 4;
+  constexpr int LD = sym_ld(TS);
+  constexpr int PS = NW * 16 * LD;
+  extern __shared__ __align__(16) unsigned char symh_sm[];
+  ulonglong2* s0 = reinterpret_cast<ulonglong2*>(symh_sm);
+  ulonglong2* s1 = s0 + TS;
+  ulonglong2* s2 = s1 + TS;
+  ulonglong2* s3 = s2 + TS;
+  ulonglong2* s4 = s3 + TS;
+  ulonglong2* s5 = s4 + TS;
+  float* sT = reinterpret_cast<float*>(s5 + TS);  // [4][NW][16][LD]
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lr = lane & 15, ls = lane >> 4;
+  const int U = a.work_box[blockIdx.x];
+  const int row0 = a.work_row[blockIdx.x];
+  const int64_t offU = a.box_off[U];
+  const int bsU = (int)(a.box_off[U + 1] - offU);
+  const int rU = a.box_rank[U];
+  const int wrow0 = row0 + 64 * warp;
+  const bool active = wrow0 < bsU;
+  const int64_t pbase = a.box_pbase[U] + (int64_t)(row0 / 256) * a.box_pstride[U];
+  const float kc = kappa * 0.15915494309189535f;
+  const f2_t kc2 = f2_pack(kc, kc);
+
+  f2_t thx[kSymPairs], thy[kSymPairs], thz[kSymPairs], tlx[kSymPairs], tly[kSymPairs], tlz[kSymPairs];
+#pragma unroll
+  for (int p = 0; p < kSymPairs; ++p) {
+    const int ra = wrow0 + lr + 32 * p, rb = ra + 16;
+    const int64_t ea = offU + max(0, min(ra, bsU - 1)), eb = offU + max(0, min(rb, bsU - 1));
+    const float4 ha = a.hi32[ea], hb = a.hi32[eb];
+    const float4 la = a.lo32[ea], lb = a.lo32[eb];
+    thx[p] = f2_pack(ha.x, hb.x);
+    thy[p] = f2_pack(ha.y, hb.y);
+    thz[p] = f2_pack(ha.z, hb.z);
+    tlx[p] = f2_pack(la.x, lb.x);
+    tly[p] = f2_pack(la.y, lb.y);
+    tlz[p] = f2_pack(la.z, lb.z);
+  }
+  const bool skel_rows = wrow0 < rU;
+  const f2_t zero = 0ull;
+  f2_t sur[kSymPairs], cur[kSymPairs], sui[kSymPairs], cui[kSymPairs];
+  f2_t shr[kSymPairs], chr[kSymPairs], shi[kSymPairs], chi[kSymPairs];
+#pragma unroll
+  for (int p = 0; p < kSymPairs; ++p) sur[p] = cur[p] = sui[p] = cui[p] = shr[p] = chr[p] = shi[p] = chi[p] = zero;
+
+  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
+  for (int64_t l = l0; l < l1; ++l) {
+    const int s = a.list_src[l];
+    const int kind = a.list_kind[l];
+    const int64_t offS = a.box_off[s];
+    const int bsS = (int)(a.box_off[s + 1] - offS);
+    const int rS = a.box_rank[s];
+    const bool self = (s == U);
+    const int nh = (kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_DOWN)
+                       ? rS
+                       : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
+    const float* c1src = (kind == SKF_KIND_COARSE_DOWN) ? a.qd32 : a.q32;
+    // complex charges of A's rows seen from B (mirror kind), for the B-side sums
+    SymhCharges cT;
+#pragma unroll
+    for (int p = 0; p < kSymPairs; ++p) cT.c1r[p] = cT.c1i[p] = cT.m1i[p] = cT.c2r[p] = cT.c2i[p] = cT.m2i[p] = zero;
+    if (!self) {
+      const float* t1 = (kind == SKF_KIND_COARSE_UP) ? a.qd32 : a.q32;
+#pragma unroll
+      for (int p = 0; p < kSymPairs; ++p) {
+        const int ra = wrow0 + lr + 32 * p, rb = ra + 16;
+        float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
+        if (ra < bsU) {
+          ar = t1[2 * (offU + ra)];
+          ai = t1[2 * (offU + ra) + 1];
+        }
+        if (rb < bsU) {
+          br = t1[2 * (offU + rb)];
+          bi = t1[2 * (offU + rb) + 1];
+        }
+        cT.c1r[p] = f2_pack(ar, br);
+        cT.c1i[p] = f2_pack(ai, bi);
+        cT.m1i[p] = f2_pack(-ai, -bi);
+        float dr = 0.f, di = 0.f, er = 0.f, ei = 0.f;
+        if (kind == SKF_KIND_COLLEAGUE) {
+          if (ra < bsU) {
+            dr = a.qhn32[2 * (offU + ra)];
+            di = a.qhn32[2 * (offU + ra) + 1];
+          }
+          if (rb < bsU) {
+            er = a.qhn32[2 * (offU + rb)];
+            ei = a.qhn32[2 * (offU + rb) + 1];
+          }
+        } else if (kind == SKF_KIND_COARSE_DOWN) {
+          dr = -ar;
+          di = -ai;
+          er = -br;
+          ei = -bi;
+        }
+        cT.c2r[p] = f2_pack(dr, er);
+        cT.c2i[p] = f2_pack(di, ei);
+        cT.m2i[p] = f2_pack(-di, -ei);
+      }
+    }
+    const bool row_h_kind = kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_UP;
+    const bool t_h_kind = kind == SKF_KIND_COLLEAGUE ? skel_rows : kind == SKF_KIND_COARSE_DOWN;
+    const int64_t pblk = self ? 0 : pbase + a.list_poff[l];
+    for (int t0 = 0; t0 < bsS;) {
+      const bool hseg = t0 < nh;
+      const int nt = min(TS, (hseg ? nh : bsS) - t0);
+      __syncthreads();
+      for (int j = threadIdx.x; j < nt; j += NW * 32) {
+        const int64_t e = offS + t0 + j;
+        const float4 h = a.hi32[e], lo = a.lo32[e];
+        const float c1r = c1src[2 * e], c1i = c1src[2 * e + 1];
+        float c2r = 0.f, c2i = 0.f;
+        if (kind == SKF_KIND_COLLEAGUE) {
+          c2r = a.qhn32[2 * e];
+          c2i = a.qhn32[2 * e + 1];
+        } else if (kind == SKF_KIND_COARSE_UP) {
+          c2r = -c1r;
+          c2i = -c1i;
+        }
+        s0[j] = make_ulonglong2(f2_pack(-h.x, -h.x), f2_pack(-h.y, -h.y));
+        s1[j] = make_ulonglong2(f2_pack(-h.z, -h.z), f2_pack(-lo.x, -lo.x));
+        s2[j] = make_ulonglong2(f2_pack(-lo.y, -lo.y), f2_pack(-lo.z, -lo.z));
+        s3[j] = make_ulonglong2(f2_pack(c1r, c1r), f2_pack(c1i, c1i));
+        s4[j] = make_ulonglong2(f2_pack(-c1i, -c1i), f2_pack(c2r, c2r));
+        s5[j] = make_ulonglong2(f2_pack(c2i, c2i), f2_pack(-c2i, -c2i));
+      }
+      __syncthreads();
+      const bool hr = active && hseg && row_h_kind && skel_rows;
+      const bool ht = active && hseg && t_h_kind;
+      f2_t pur[kSymPairs], pui[kSymPairs], phr[kSymPairs], phi[kSymPairs];
+#pragma unroll
+      for (int p = 0; p < kSymPairs; ++p) pur[p] = pui[p] = phr[p] = phi[p] = zero;
+      float* tw = sT + warp * 16 * LD;
+      if (active) {
+        if (self) {
+          if (hr) symh_tile<true, false, false, true, LD>(s0, s1, s2, s3, s4, s5, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, kc2, cT, pur, pui, phr, phi, tw);
+          else symh_tile<false, false, false, true, LD>(s0, s1, s2, s3, s4, s5, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, kc2, cT, pur, pui, phr, phi, tw);
+        } else if (hr) {
+          if (ht) symh_tile<true, true, true, false, LD>(s0, s1, s2, s3, s4, s5, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, kc2, cT, pur, pui, phr, phi, tw);
+          else symh_tile<true, false, true, false, LD>(s0, s1, s2, s3, s4, s5, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, kc2, cT, pur, pui, phr, phi, tw);
+        } else {
+          if (ht) symh_tile<false, true, true, false, LD>(s0, s1, s2, s3, s4, s5, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, kc2, cT, pur, pui, phr, phi, tw);
+          else symh_tile<false, false, true, false, LD>(s0, s1, s2, s3, s4, s5, nt, ls, lr, thx, thy, thz, tlx, tly, tlz, kc2, cT, pur, pui, phr, phi, tw);
+        }
+#pragma unroll
+        for (int p = 0; p < kSymPairs; ++p) {
+          f2_two_sum(sur[p], cur[p], pur[p]);
+          f2_two_sum(sui[p], cui[p], pui[p]);
+          if (hr) {
+            f2_two_sum(shr[p], chr[p], phr[p]);
+            f2_two_sum(shi[p], chi[p], phi[p]);
+          }
+        }
+      }
+      if (!self) {
+        // warps without rows, or without B-side uh sums, contribute zeros
+        if (!active || !ht) {
+          for (int k = lane; k < 16 * TS; k += 32) {
+            const int rr = k / TS, jj = k - rr * TS;
+            if (jj < nt) {
+              if (!active) {
+                tw[rr * LD + jj] = 0.f;
+                tw[PS + rr * LD + jj] = 0.f;
+              }
+              tw[2 * PS + rr * LD + jj] = 0.f;
+              tw[3 * PS + rr * LD + jj] = 0.f;
+            }
+          }
+        }
+        __syncthreads();
+        // item i < 4 TS: partial array i / TS (u re, u im, uh re, uh im) of
+        // source i % TS; 4 warps x 16 lanes each
+        for (int i = threadIdx.x; i < 4 * TS; i += NW * 32) {
+          const int part = i / TS, j = i - part * TS;
+          if (j < nt) {
+            const float* src = sT + part * PS;
+            float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+              v0 += src[(0 * 16 + r) * LD + j];
+              v1 += src[(1 * 16 + r) * LD + j];
+              v2 += src[(2 * 16 + r) * LD + j];
+              v3 += src[(3 * 16 + r) * LD + j];
+            }
+            a.pbuf[pblk + (int64_t)part * bsS + t0 + j] = (v0 + v1) + (v2 + v3);
+          }
+        }
+      }
+      t0 += nt;
+    }
+  }
+  // combine the row sums of the 2 lanes sharing rows (ls = 0, 1), in FP64
+#pragma unroll
+  for (int p = 0; p < kSymPairs; ++p) {
+    double v[8];
+    float x0, x1, y0, y1;
+    f2_unpack(sur[p], x0, x1);
+    f2_unpack(cur[p], y0, y1);
+    v[0] = (double)x0 + (double)y0;
+    v[1] = (double)x1 + (double)y1;
+    f2_unpack(sui[p], x0, x1);
+    f2_unpack(cui[p], y0, y1);
+    v[2] = (double)x0 + (double)y0;
+    v[3] = (double)x1 + (double)y1;
+    f2_unpack(shr[p], x0, x1);
+    f2_unpack(chr[p], y0, y1);
+    v[4] = (double)x0 + (double)y0;
+    v[5] = (double)x1 + (double)y1;
+    f2_unpack(shi[p], x0, x1);
+    f2_unpack(chi[p], y0, y1);
+    v[6] = (double)x0 + (double)y0;
+    v[7] = (double)x1 + (double)y1;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], 16);
+    if (active && ls == 0) {
+      const int ra = wrow0 + lr + 32 * p, rb = ra + 16;
+      if (ra < bsU) {
+        const int64_t e = offU + ra;
+        const bool sk = ra < rU;
+        a.u[2 * e] = v[0];
+        a.u[2 * e + 1] = v[2];
+        a.uh[2 * e] = sk ? v[4] : 0.0;
+        a.uh[2 * e + 1] = sk ? v[6] : 0.0;
+      }
+      if (rb < bsU) {
+        const int64_t e = offU + rb;
+        const bool sk = rb < rU;
+        a.u[2 * e] = v[1];
+        a.u[2 * e + 1] = v[3];
+        a.uh[2 * e] = sk ? v[5] : 0.0;
+        a.uh[2 * e + 1] = sk ? v[7] : 0.0;
+      }
+    }
+  }
+}
+
+// Complex form of k_sym_reduce: a partial block holds u re, u im, uh re,
+// uh im of the box's entries back to back.
+__global__ void __launch_bounds__(256) k_sym_reduce_c(const int64_t* __restrict__ box_off,
+                                                      const int32_t* __restrict__ box_rank,
+                                                      const int64_t* __restrict__ in_off,
+                                                      const int64_t* __restrict__ in_blk,
+                                                      const float* __restrict__ pbuf, double* __restrict__ u,
+                                                      double* __restrict__ uh) {
+  const int B = blockIdx.x;
+  const int64_t off = box_off[B];
+  const int bs = (int)(box_off[B + 1] - off);
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  const int64_t k0 = in_off[B], k1 = in_off[B + 1];
+  if (j >= bs || k0 == k1) return;
+  const int r = box_rank[B];
+  double ur = 0.0, ui = 0.0, hr = 0.0, hi = 0.0;
+  for (int64_t k = k0; k < k1; ++k) {
+    const int64_t b0 = in_blk[k];
+    ur += (double)pbuf[b0 + j];
+    ui += (double)pbuf[b0 + bs + j];
+    hr += (double)pbuf[b0 + 2 * bs + j];
+    hi += (double)pbuf[b0 + 3 * bs + j];
+  }
+  u[2 * (off + j)] += ur;
+  u[2 * (off + j) + 1] += ui;
+  if (j < r) {
+    uh[2 * (off + j)] += hr;
+    uh[2 * (off + j) + 1] += hi;
+  }
+}
+
 // Adds the B-side partial sums into u / uh in a fixed order.  Block
 // (box, chunk): entries [256 chunk, 256 chunk + 256) of the box.
 template <bool LOG>

@@ -91,7 +91,7 @@ def test_packed_and_scalar_mixed_kernels_agree(name):
     assert relinf(y_packed, d["y_batched"]) < 2e-6
 
 
-@pytest.mark.parametrize("name", ["lap2d_square", "lap2d_annulus", "lap3d_cube", "lap3d_sphere"])
+@pytest.mark.parametrize("name", ["lap2d_square", "lap2d_annulus", "lap3d_cube", "lap3d_sphere", "helm3d_sphere"])
 def test_symmetric_translations_agree(name):
     """Evaluating each kernel block once for both directions (symmetric path)
     gives the same apply as evaluating every direction separately."""
@@ -111,3 +111,24 @@ def test_symmetric_translations_agree(name):
     y2 = np.empty_like(x)
     plan.apply_host(x, y2, _lib.PREC_MIXED)
     assert np.array_equal(y2, y_sym)  # deterministic
+
+
+@pytest.mark.parametrize("name", ["lap3d_cube", "helm3d_sphere"])
+def test_symmetric_tile_shapes_agree(name):
+    """Every tile shape of the symmetric kernel (sources per tile, blocks per
+    SM) gives the same apply up to the order of the partial sums."""
+    from skelfmm_gb300 import _lib
+
+    d, plan = _plan(name)
+    x = np.ascontiguousarray(d["x"])
+    ys = []
+    for shape in range(4):
+        plan.set_option(_lib.OPT_SYM_SHAPE, shape)
+        y = np.empty_like(x)
+        plan.apply_host(x, y, _lib.PREC_MIXED)
+        ys.append(y)
+    plan.set_option(_lib.OPT_SYM_SHAPE, 0)
+    for y in ys[1:]:
+        assert relinf(y, ys[0]) < 1e-6
+    assert relinf(ys[0], d["y_batched"]) < 2e-6
+
