@@ -264,7 +264,7 @@ class CalibratedRankPredictor:
     while a few more sketch rows cost little.  The predicted rank is then
     ``margin`` above the corrected estimate, capped at the box size."""
 
-    def __init__(self, margin=10, calibrate=0.9, calibrate_big=0.98, big_box=256):
+    def __init__(self, margin=16, calibrate=0.9, calibrate_big=0.995, big_box=256):
         self.margin = int(margin)
         self.calibrate = calibrate
         self.calibrate_big = calibrate_big
@@ -314,7 +314,7 @@ class LearnedRankPredictor(CalibratedRankPredictor):
     """The rank network's estimate (``RankMLP`` on ``level_features``),
     calibrated level by level.  It sets the sketch size of every box."""
 
-    def __init__(self, model: RankMLP, margin=10, calibrate=0.9, calibrate_big=0.98, big_box=256):
+    def __init__(self, model: RankMLP, margin=16, calibrate=0.9, calibrate_big=0.995, big_box=256):
         super().__init__(margin, calibrate, calibrate_big, big_box)
         self.model = model
 
