@@ -223,7 +223,7 @@ struct QrScratch {
 };
 
 // Real reflector I - tau v v^T on rows k..m-1 of columns held in registers.
-// A group of G lanes (G = 8, 16 or 32, group lane sl) holds one column, CR
+// A group of G lanes (G = 4, 8, 16 or 32, group lane sl) holds one column, CR
 // rows per lane (row k + sl + G q, m - k <= G CR), loaded with every load in
 // flight: a step costs one round trip to L2 per column.  The narrowest group
 // whose registers hold the slice is used, so the FP64 instructions issued per
@@ -327,12 +327,17 @@ __device__ __noinline__ void reflect_trailing(double* A, int m, int n, int k, co
 __device__ __forceinline__ bool reflect_trailing_regs(double* A, int m, int n, int k, const double* vv, double tau,
                                                       double* vn1, double* vn2, double tol3z) {
   const int len = m - k;
-  if (len <= 8 * kColRegs) {
+  if (len <= 4 * kColRegs) {
+    const int cr = (len + 3) / 4;
+    if (cr <= 4) reflect_trailing<4, 4>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 8) reflect_trailing<4, 8>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 12) reflect_trailing<4, 12>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 16) reflect_trailing<4, 16>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else if (cr <= 20) reflect_trailing<4, 20>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    else reflect_trailing<4, 24>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+  } else if (len <= 8 * kColRegs) {
     const int cr = (len + 7) / 8;
-    if (cr <= 4) reflect_trailing<8, 4>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
-    else if (cr <= 8) reflect_trailing<8, 8>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
-    else if (cr <= 12) reflect_trailing<8, 12>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
-    else if (cr <= 16) reflect_trailing<8, 16>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
+    if (cr <= 16) reflect_trailing<8, 16>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
     else if (cr <= 20) reflect_trailing<8, 20>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
     else reflect_trailing<8, 24>(A, m, n, k, vv, tau, vn1, vn2, tol3z);
   } else if (len <= 16 * kColRegs) {
