@@ -164,6 +164,21 @@ __device__ __forceinline__ void ff_add_prod(FF& acc, float ah, float al, float b
 __device__ __forceinline__ void ff_sub_prod(FF& acc, float ah, float al, float bh, float bl) {
   ff_add_prod(acc, -ah, -al, bh, bl);
 }
+// Warp sum of float-float values on the FP32 pipes (xor butterfly, TwoSum of
+// the leading parts): lane 0's result is the same on every run.
+__device__ __forceinline__ double ff_warp_sum(FF a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, a.s, o);
+    const float c2 = __shfl_xor_sync(0xffffffffu, a.c, o);
+    const float t = a.s + s2;
+    const float z = t - a.s;
+    const float err = (a.s - (t - z)) + (s2 - z);
+    a.s = t;
+    a.c = (a.c + c2) + err;
+  }
+  return (double)a.s + (double)a.c;
+}
 __device__ __forceinline__ void split_f64(double v, float& h, float& l) {
   h = (float)v;
   l = (float)(v - (double)h);
@@ -205,8 +220,8 @@ __global__ void __launch_bounds__(256) k_up_ff(const int32_t* __restrict__ boxes
         ff_add_prod(ar, Th[rb + c], Tl[rb + c], xh[c], xl[c]);
       }
     }
-    const double sr = warp_sum((double)ar.s + (double)ar.c);
-    const double si = C ? warp_sum((double)ai.s + (double)ai.c) : 0.0;
+    const double sr = ff_warp_sum(ar);
+    const double si = C ? ff_warp_sum(ai) : 0.0;
     if (lane == 0) {
       const int64_t e = off + i;
       const int64_t ps = pslot[e];

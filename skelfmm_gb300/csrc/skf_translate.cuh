@@ -1412,19 +1412,30 @@ __global__ void __launch_bounds__(256) k_sym_reduce_c(const int64_t* __restrict_
   const int64_t k0 = in_off[B], k1 = in_off[B + 1];
   if (j >= bs || k0 == k1) return;
   const int r = box_rank[B];
-  double ur = 0.0, ui = 0.0, hr = 0.0, hi = 0.0;
-  for (int64_t k = k0; k < k1; ++k) {
-    const int64_t b0 = in_blk[k];
-    ur += (double)pbuf[b0 + j];
-    ui += (double)pbuf[b0 + bs + j];
-    hr += (double)pbuf[b0 + 2 * bs + j];
-    hi += (double)pbuf[b0 + 3 * bs + j];
+  double ur[2] = {0.0, 0.0}, ui[2] = {0.0, 0.0}, hr[2] = {0.0, 0.0}, hi[2] = {0.0, 0.0};
+  int64_t k = k0;
+  for (; k + 1 < k1; k += 2) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int64_t b = in_blk[k + q];
+      ur[q] += (double)pbuf[b + j];
+      ui[q] += (double)pbuf[b + bs + j];
+      hr[q] += (double)pbuf[b + 2 * bs + j];
+      hi[q] += (double)pbuf[b + 3 * bs + j];
+    }
   }
-  u[2 * (off + j)] += ur;
-  u[2 * (off + j) + 1] += ui;
+  if (k < k1) {
+    const int64_t b = in_blk[k];
+    ur[0] += (double)pbuf[b + j];
+    ui[0] += (double)pbuf[b + bs + j];
+    hr[0] += (double)pbuf[b + 2 * bs + j];
+    hi[0] += (double)pbuf[b + 3 * bs + j];
+  }
+  u[2 * (off + j)] += ur[0] + ur[1];
+  u[2 * (off + j) + 1] += ui[0] + ui[1];
   if (j < r) {
-    uh[2 * (off + j)] += hr;
-    uh[2 * (off + j) + 1] += hi;
+    uh[2 * (off + j)] += hr[0] + hr[1];
+    uh[2 * (off + j) + 1] += hi[0] + hi[1];
   }
 }
 
@@ -1445,22 +1456,25 @@ __global__ void __launch_bounds__(256) k_sym_reduce(const int64_t* __restrict__ 
   if (j >= bs || k0 == k1) return;
   const int r = box_rank[B];
   const double scale = LOG ? 0.34657359027997264 : 1.0;
-  double su0 = 0.0, su1 = 0.0, sh0 = 0.0, sh1 = 0.0;
+  // four independent chains keep eight loads in flight per thread; the
+  // grouping is fixed, so the sum is deterministic
+  double su[4] = {0.0, 0.0, 0.0, 0.0}, sh[4] = {0.0, 0.0, 0.0, 0.0};
   int64_t k = k0;
-  for (; k + 1 < k1; k += 2) {
-    const int64_t b0 = in_blk[k], b1 = in_blk[k + 1];
-    su0 += (double)pbuf[b0 + j];
-    su1 += (double)pbuf[b1 + j];
-    sh0 += (double)pbuf[b0 + bs + j];
-    sh1 += (double)pbuf[b1 + bs + j];
+  for (; k + 3 < k1; k += 4) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t b = in_blk[k + q];
+      su[q] += (double)pbuf[b + j];
+      sh[q] += (double)pbuf[b + bs + j];
+    }
   }
-  if (k < k1) {
-    const int64_t b0 = in_blk[k];
-    su0 += (double)pbuf[b0 + j];
-    sh0 += (double)pbuf[b0 + bs + j];
+  for (int q = 0; k < k1; ++k, ++q) {
+    const int64_t b = in_blk[k];
+    su[q] += (double)pbuf[b + j];
+    sh[q] += (double)pbuf[b + bs + j];
   }
-  u[off + j] += scale * (su0 + su1);
-  if (j < r) uh[off + j] += scale * (sh0 + sh1);
+  u[off + j] += scale * ((su[0] + su[1]) + (su[2] + su[3]));
+  if (j < r) uh[off + j] += scale * ((sh[0] + sh[1]) + (sh[2] + sh[3]));
 }
 
 }  // namespace skf
