@@ -1482,8 +1482,12 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
       if (status == SKF_OK) {
         std::vector<int8_t> hs(nb), done(nb, 0);
         for (int32_t lb : clustered) done[lb] = 1;
-        SKF_CUDA_TRY(cudaMemcpyAsync(hs.data(), dstat + b0, nb, cudaMemcpyDeviceToHost, st));
-        SKF_CUDA_TRY(cudaStreamSynchronize(st));
+        cudaError_t ce = cudaMemcpyAsync(hs.data(), dstat + b0, nb, cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) {
+          set_last_cuda_error(ce);
+          status = SKF_ERR_CUDA;
+        }
         for (int32_t lb : rnd)
           if (hs[lb] % 10 == 2 && !done[lb]) full.push_back(lb);
       }
