@@ -252,3 +252,29 @@ def test_network_gains_over_calibrated_constant():
     fb_l = sum(s["fallback"] for s in fl.level_stats.values())
     assert fb_l < 0.02 * kept_l, (fb_l, kept_l)
     assert wl < 0.6 * wc and wl < 0.4 * wf, (wl, wc, wf)
+
+
+def test_learned_build_complex_operator():
+    """The learned-rank build on a complex operator (3D Helmholtz on the
+    sphere): the complex sketch, residual check and deferred fallback give an
+    apply within the pivoted-QR build's accuracy."""
+    from skelfmm_gb300 import operators
+    from skelfmm_gb300.skel_fmm import SkelFMM, direct_sum
+    from skelfmm_gb300.tree import get_point_dist
+
+    n = 30000
+    pts = get_point_dist(n, "sphere_surface", rng=np.random.default_rng(5))
+    rs = np.random.RandomState(2)
+    x = rs.randn(n) + 1j * rs.randn(n)
+    idx = np.random.default_rng(1).choice(n, 200, replace=False)
+    yd = direct_sum(operators.HELMHOLTZ_3D, pts, x, idx, param=5.0)
+    errs, stats = {}, {}
+    for learned in (False, True):
+        f = SkelFMM(pts, operators.HELMHOLTZ_3D, tol=1e-6, leaf_size=128, param=5.0, learned_rank=learned,
+                    keep_host_fmm=True).build()
+        y = f.apply(x)
+        errs[learned] = float(np.abs(y[idx] - yd).max() / np.abs(yd).max())
+        stats[learned] = f.fmm.level_stats
+    randomized = sum(s.get("randomized", 0) for s in stats[True].values())
+    assert randomized > 0
+    assert errs[True] <= max(3 * errs[False], 1e-6), errs
