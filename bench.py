@@ -178,6 +178,18 @@ def dist_setup():
     return None, 0, 1
 
 
+def reduce_over_ranks(dist, value, op, device):
+    """A per-rank number combined over all ranks: "max" (replicas finish with
+    their slowest rank) or "sum" (units processed by all ranks); the rank's
+    own value when there is one rank."""
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def cpu_baseline_sample(rb, x, opname="laplace_3d", kappa=0.0, budget_s=15.0):
     """Reference algorithm (oracle port: FP64 dense kernel blocks) on the host
     cores, over a sample of target boxes of the same ragged build; throughput
@@ -308,10 +320,7 @@ def run_single(args):
     with ClockSampler(dev.index) as clk:
         ms_mixed, ms_list = timed(_lib.PREC_MIXED, args.steps, args.warmup)
     clocks = clk.summary()
-    ms_t = torch.tensor([ms_mixed], device=dev)
-    if dist is not None:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_step = float(ms_t.item())
+    ms_step = reduce_over_ranks(dist, ms_mixed, "max", dev)
 
     # e2e through the C ABI with pinned host buffers
     xh = torch.from_numpy(x).pin_memory()
@@ -323,11 +332,7 @@ def run_single(args):
     for _ in range(args.steps):
         plan.apply_host(xh, yh, _lib.PREC_MIXED, sp)
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_t = torch.tensor([e2e_s], device=dev)
-    if dist is not None:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_s = float(e2e_t.item())
+    e2e_s = reduce_over_ranks(dist, (time.perf_counter() - t0) / args.steps, "max", dev)
 
     # plain FP64 apply (the parity path) for the mixed/FP64 ratio
     ms_fp64 = None
@@ -417,6 +422,8 @@ def run_batch(args):
         b._graph.replay()
     torch.cuda.synchronize(dev)
     evs = []
+    if dist is not None:
+        dist.barrier()
     with ClockSampler(dev.index) as clk:
         for _ in range(args.steps):
             flush.zero_()
@@ -427,7 +434,9 @@ def run_batch(args):
             e1.record(stream)
             evs.append((e0, e1))
         torch.cuda.synchronize(dev)
-    ms_step = float(np.mean([a.elapsed_time(c) for a, c in evs]))
+    if dist is not None:
+        dist.barrier()
+    ms_step = reduce_over_ranks(dist, float(np.mean([a.elapsed_time(c) for a, c in evs])), "max", dev)
     # e2e: pinned host charges in, graph replay, potentials out
     xh = torch.from_numpy(np.concatenate(xs)).pin_memory()
     yh = torch.empty_like(xh).pin_memory()
@@ -438,7 +447,7 @@ def run_batch(args):
         b._graph.replay()
         yh.copy_(b._y, non_blocking=True)
         torch.cuda.synchronize(dev)
-    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = reduce_over_ranks(dist, (time.perf_counter() - t0) / args.steps, "max", dev)
     ys = b.apply(xs)
     errs = b.relerr(xs, ys, ncheck=200)
     xs32 = [v.astype(np.float32) for v in xs]
@@ -448,7 +457,9 @@ def run_batch(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(b.plan.rb, np.concatenate(xs), "laplace_2d", 0.0)
-    value = ntot * ws / (ms_step * 1e-3) / 1e6
+    # ranks hold different instances: the job's units are summed over ranks
+    nall = reduce_over_ranks(dist, ntot, "sum", dev)
+    value = nall / (ms_step * 1e-3) / 1e6
     line = {
         "metric": METRIC["batch64_annulus"], "value": round(value, 2), "unit": "Mpts/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
@@ -458,7 +469,7 @@ def run_batch(args):
                    "tuned_scheme": {"symmetric": int(b.plan.tuned[0]), "packed_shape": int(b.plan.tuned[1])},
                    "l2": "256 MB buffer zeroed between timed steps (outside the step events)",
                    "parallelism": f"replicas x{ws}"},
-        "e2e": {"value": round(ntot * ws / e2e_s / 1e6, 2), "unit": "Mpts/s", "h2d_bytes_per_step": ntot * 8,
+        "e2e": {"value": round(nall / e2e_s / 1e6, 2), "unit": "Mpts/s", "h2d_bytes_per_step": ntot * 8,
                 "d2h_bytes_per_step": ntot * 8, "ms_per_step": round(e2e_s * 1e3, 3)},
         "gpu_launches": int(b.plan.info.launches_mixed) * args.steps,
         "gpu_launches_per_step": int(b.plan.info.launches_mixed),
