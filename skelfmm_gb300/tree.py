@@ -106,13 +106,20 @@ class BalancedTree:
         D = _MAX_DEPTH[ndim]
         self._depth = D
         corner = self.c0 - 0.5 * self.L0
-        scaled = (XX - corner[None, :]) / self.L0 * float(1 << D)
-        q = np.clip(np.floor(scaled), 0, (1 << D) - 1).astype(np.int64)
+        # (x - corner) / L0 * 2^D, floored and clipped to [0, 2^D - 1], in place
+        scaled = XX - corner[None, :]
+        scaled /= self.L0
+        scaled *= float(1 << D)
+        np.floor(scaled, out=scaled)
+        np.minimum(scaled, float((1 << D) - 1), out=scaled)
+        np.maximum(scaled, 0.0, out=scaled)
+        q = scaled.astype(np.int64)
+        del scaled
         keys = morton_encode(q, D)
         perm = np.argsort(keys, kind="stable")
         self._perm = perm
         self._skeys = keys[perm]
-        self._sq = q[perm]
+        self._q = q  # integer coordinates in input order (box corners via _perm)
 
         # per level (sorted by Morton code): coords, codes, point ranges, leaf flags
         self._Lc = [np.zeros((1, ndim), dtype=np.int64)]
@@ -156,19 +163,20 @@ class BalancedTree:
         starts = self._Ls[lev][sel]
         ends = self._Le[lev][sel]
         lens = ends - starts
+        shift = np.uint64(self.ndim * (D - lev - 1))
         if sel.size == self._Ls[lev].shape[0] and int(lens.sum()) == self.N:
             idx = np.arange(self.N, dtype=np.int64)
+            ck = self._skeys >> shift
         else:
             # concatenated point ranges [start, end) of the boxes
             before = np.cumsum(lens) - lens
             idx = np.arange(int(lens.sum()), dtype=np.int64) + np.repeat(starts - before, lens)
-        shift = np.uint64(self.ndim * (D - lev - 1))
-        ck = self._skeys[idx] >> shift
+            ck = self._skeys[idx] >> shift
         brk = np.flatnonzero((ck[1:] != ck[:-1]) | (idx[1:] != idx[:-1] + 1)) + 1
         first = np.concatenate(([0], brk))
         cs = idx[first]
         ce = np.concatenate((idx[brk - 1] + 1, [idx[-1] + 1]))
-        coords = (self._sq[cs] >> (D - lev - 1)).astype(np.int64)
+        coords = (self._q[self._perm[cs]] >> (D - lev - 1)).astype(np.int64)
         codes = ck[first]
         self._Lleaf[lev][sel] = False
         if len(self._Lk) <= lev + 1:
