@@ -165,17 +165,22 @@ class BalancedTree:
         lens = ends - starts
         shift = np.uint64(self.ndim * (D - lev - 1))
         if sel.size == self._Ls[lev].shape[0] and int(lens.sum()) == self.N:
-            idx = np.arange(self.N, dtype=np.int64)
+            # every box of the level splits: the points in order, child
+            # boundaries where the child code changes
             ck = self._skeys >> shift
+            brk = np.flatnonzero(ck[1:] != ck[:-1]) + 1
+            first = np.concatenate(([0], brk)).astype(np.int64)
+            cs = first
+            ce = np.concatenate((brk, [self.N])).astype(np.int64)
         else:
             # concatenated point ranges [start, end) of the boxes
             before = np.cumsum(lens) - lens
             idx = np.arange(int(lens.sum()), dtype=np.int64) + np.repeat(starts - before, lens)
             ck = self._skeys[idx] >> shift
-        brk = np.flatnonzero((ck[1:] != ck[:-1]) | (idx[1:] != idx[:-1] + 1)) + 1
-        first = np.concatenate(([0], brk))
-        cs = idx[first]
-        ce = np.concatenate((idx[brk - 1] + 1, [idx[-1] + 1]))
+            brk = np.flatnonzero((ck[1:] != ck[:-1]) | (idx[1:] != idx[:-1] + 1)) + 1
+            first = np.concatenate(([0], brk))
+            cs = idx[first]
+            ce = np.concatenate((idx[brk - 1] + 1, [idx[-1] + 1]))
         coords = (self._q[self._perm[cs]] >> (D - lev - 1)).astype(np.int64)
         codes = ck[first]
         self._Lleaf[lev][sel] = False
