@@ -116,9 +116,16 @@ class BalancedTree:
         q = scaled.astype(np.int64)
         del scaled
         keys = morton_encode(q, D)
-        perm = np.argsort(keys, kind="stable")
+        # stable argsort: an unstable sort, then input order restored among
+        # equal keys (points sharing a finest cell; rare)
+        perm = np.argsort(keys)
+        skeys = keys[perm]
+        tie = np.flatnonzero(skeys[1:] == skeys[:-1])
+        if tie.size:
+            pos = np.unique(np.concatenate((tie, tie + 1)))
+            perm[pos] = perm[pos][np.lexsort((perm[pos], skeys[pos]))]
         self._perm = perm
-        self._skeys = keys[perm]
+        self._skeys = skeys
         self._q = q  # integer coordinates in input order (box corners via _perm)
 
         # per level (sorted by Morton code): coords, codes, point ranges, leaf flags
