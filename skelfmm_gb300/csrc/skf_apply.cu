@@ -422,6 +422,7 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
     b.hi32 = p->hi32;
     b.lo32 = p->lo32;
     b.geom32 = p->geom32;
+    b.geom32lo = p->geom32lo;
     b.q32 = p->q32;
     b.qhn32 = p->qhn32;
     b.qd32 = p->qd32;
@@ -689,15 +690,24 @@ __global__ void k_block_apply(int npairs, int mmax, int nmax, const int32_t* __r
     }
     double kr, ki;
     if (MIXED) {
-      float d[3] = {0, 0, 0};
+      // the difference as an FP32 pair dh + dl of the FP64 difference (the
+      // plan's binade-shifted hi/lo split gives the same pair to ~2^-48)
+      float d[3] = {0, 0, 0}, dh[3] = {0, 0, 0}, dl[3] = {0, 0, 0};
 #pragma unroll
       for (int c = 0; c < D; ++c) {
-        const float hx = (float)xi[c], hy = (float)yj[c];
-        const float lx = (float)(xi[c] - (double)hx), ly = (float)(yj[c] - (double)hy);
-        d[c] = (hx - hy) + (lx - ly);
+        const double dd = xi[c] - yj[c];
+        dh[c] = (float)dd;
+        dl[c] = (float)(dd - (double)dh[c]);
+        d[c] = dh[c] + dl[c];
+      }
+      float rotn = 0.f;
+      if (G != 0) {
+        const float nh[3] = {(float)gx, (float)gy, (float)gz};
+        rotn = dot_dn(dh[0], dh[1], dh[2], dl[0], dl[1], dl[2], nh[0], nh[1], nh[2], (float)(gx - (double)nh[0]),
+                      (float)(gy - (double)nh[1]), (float)(gz - (double)nh[2]));
       }
       float fr, fi;
-      eval_f32<OP>(d[0], d[1], d[2], (float)gx, (float)gy, (float)gz, kf, fr, fi);
+      eval_f32<OP>(d[0], d[1], d[2], rotn, kf, fr, fi);
       kr = fr;
       ki = fi;
     } else {

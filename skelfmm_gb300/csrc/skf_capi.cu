@@ -170,17 +170,46 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   p->nlist = L;
   for (int b = 0; b < nb; ++b) p->max_bs = std::max<int>(p->max_bs, (int)(d->box_off[b + 1] - d->box_off[b]));
 
-  // entry coordinates: FP64 (x,y,z,0) and the FP32 hi/lo split
+  for (int64_t e = 0; e < E * d->ndim; ++e)
+    if (!std::isfinite(d->entry_xyz[e])) {
+      free_plan(p);
+      return SKF_ERR_ARG;
+    }
+  if (d->entry_geom)
+    for (int64_t e = 0; e < E * 3; ++e)
+      if (!std::isfinite(d->entry_geom[e])) {
+        free_plan(p);
+        return SKF_ERR_ARG;
+      }
+  // entry coordinates: FP64 (x,y,z,0) and the FP32 hi/lo split.  The split
+  // is taken of the coordinates translated into one binade [B, 2B), B a power
+  // of two above the extent of the entries: every hi then lies on the same
+  // FP32 grid (spacing B 2^-23), so hi_i - hi_j is exact for every pair and
+  // d = (hi_i - hi_j) + (lo_i - lo_j) carries d to ~B 2^-48 absolute.  The
+  // kernels only use differences, so the translation changes nothing else.
+  double cmin[3] = {0, 0, 0}, cmax[3] = {0, 0, 0};
+  for (int k = 0; k < d->ndim; ++k) {
+    cmin[k] = cmax[k] = d->entry_xyz[k];
+    for (int64_t e = 1; e < E; ++e) {
+      const double c = d->entry_xyz[e * d->ndim + k];
+      cmin[k] = std::min(cmin[k], c);
+      cmax[k] = std::max(cmax[k], c);
+    }
+  }
+  double extent = 0.0;
+  for (int k = 0; k < d->ndim; ++k) extent = std::max(extent, cmax[k] - cmin[k]);
+  const double B = extent > 0.0 ? std::ldexp(1.0, std::ilogb(extent) + 1) : 1.0;
   std::vector<double4_32a> xyz(E);
   std::vector<float4> hi(E), lo(E);
   for (int64_t e = 0; e < E; ++e) {
     double c[3] = {0, 0, 0};
     for (int k = 0; k < d->ndim; ++k) c[k] = d->entry_xyz[e * d->ndim + k];
     xyz[e] = make_double4_32a(c[0], c[1], c[2], 0.0);
-    float h[3], l[3];
-    for (int k = 0; k < 3; ++k) {
-      h[k] = (float)c[k];
-      l[k] = (float)(c[k] - (double)h[k]);
+    float h[3] = {0, 0, 0}, l[3] = {0, 0, 0};
+    for (int k = 0; k < d->ndim; ++k) {
+      const double s = (c[k] - cmin[k]) + B;
+      h[k] = (float)s;
+      l[k] = (float)(s - (double)h[k]);
     }
     hi[e] = make_float4(h[0], h[1], h[2], 0.f);
     lo[e] = make_float4(l[0], l[1], l[2], 0.f);
@@ -189,14 +218,19 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   SKF_TRY(upload(p, &p->hi32, hi.data(), E));
   SKF_TRY(upload(p, &p->lo32, lo.data(), E));
   if (d->entry_geom) {
+    // normals as FP64 and as an FP32 pair (hi = fl32(n), lo = fl32(n - hi)):
+    // the double-layer kernels form (x - y).n from the pair (see dot_dn)
     std::vector<double4_32a> g(E);
-    std::vector<float4> g32(E);
+    std::vector<float4> g32(E), g32lo(E);
     for (int64_t e = 0; e < E; ++e) {
       g[e] = make_double4_32a(d->entry_geom[3 * e], d->entry_geom[3 * e + 1], d->entry_geom[3 * e + 2], 0.0);
       g32[e] = make_float4((float)g[e].x, (float)g[e].y, (float)g[e].z, 0.f);
+      g32lo[e] = make_float4((float)(g[e].x - (double)g32[e].x), (float)(g[e].y - (double)g32[e].y),
+                             (float)(g[e].z - (double)g32[e].z), 0.f);
     }
     SKF_TRY(upload(p, &p->geom64, g.data(), E));
     SKF_TRY(upload(p, &p->geom32, g32.data(), E));
+    SKF_TRY(upload(p, &p->geom32lo, g32lo.data(), E));
   }
   SKF_TRY(upload(p, &p->box_off, d->box_off, (size_t)nb + 1));
   SKF_TRY(upload(p, &p->box_rank, d->box_rank, (size_t)nb));

@@ -79,9 +79,10 @@ struct skf_plan {
   // per entry
   double4_32a* xyz64 = nullptr;   // (x, y, z, 0)
   double4_32a* geom64 = nullptr;  // (nx, ny, nz, 0) or null
-  float4* hi32 = nullptr;     // fl32(x)
-  float4* lo32 = nullptr;     // fl32(x - fl32(x))
-  float4* geom32 = nullptr;
+  float4* hi32 = nullptr;     // fl32(s), s = x translated into one binade
+  float4* lo32 = nullptr;     // fl32(s - fl32(s))
+  float4* geom32 = nullptr;   // fl32(n)
+  float4* geom32lo = nullptr; // fl32(n - fl32(n))
   int64_t* pslot = nullptr;
   // leaf permutation
   int64_t* perm_entry = nullptr;

@@ -136,11 +136,46 @@ __device__ __forceinline__ void eval_f64(double dx, double dy, double dz, double
   }
 }
 
+// (x - y).n of the double-layer kernels to FP32 rounding of the result.
+// For points on a surface |(x - y).n| ~ r^2 while its terms are ~r, so a
+// plain FP32 dot product loses ~2^-24 / r relatively.  Here d = dh + dl with
+// dh exact (the hi parts of both points lie on one FP32 grid) and
+// n = nh + nl (FP32 pair): the products dh*nh are split exactly with FMA
+// residuals and summed with TwoSum (the Dot2 scheme of Ogita, Rump & Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005); the cross
+// terms dh*nl + dl*nh, ~2^-24 of the products, need only FP32.  The _rn
+// intrinsics keep the compiler from contracting the error-free steps.
+__device__ __forceinline__ float dot_dn(float dhx, float dhy, float dhz, float dlx, float dly, float dlz,
+                                        float nhx, float nhy, float nhz, float nlx, float nly, float nlz) {
+  float p = __fmul_rn(dhx, nhx);
+  float s = fmaf(dhx, nhx, -p);
+  float h = __fmul_rn(dhy, nhy);
+  float e = fmaf(dhy, nhy, -h);
+  float t = __fadd_rn(p, h);
+  float z = __fsub_rn(t, p);
+  s = __fadd_rn(s, __fadd_rn(__fadd_rn(__fsub_rn(p, __fsub_rn(t, z)), __fsub_rn(h, z)), e));
+  p = t;
+  h = __fmul_rn(dhz, nhz);
+  e = fmaf(dhz, nhz, -h);
+  t = __fadd_rn(p, h);
+  z = __fsub_rn(t, p);
+  s = __fadd_rn(s, __fadd_rn(__fadd_rn(__fsub_rn(p, __fsub_rn(t, z)), __fsub_rn(h, z)), e));
+  p = t;
+  s = fmaf(dhx, nlx, s);
+  s = fmaf(dhy, nly, s);
+  s = fmaf(dhz, nlz, s);
+  s = fmaf(dlx, nhx, s);
+  s = fmaf(dly, nhy, s);
+  s = fmaf(dlz, nhz, s);
+  return __fadd_rn(p, s);
+}
+
 // FP32 evaluation from an accurate difference vector (see the translation
-// kernel: differences are formed from hi/lo split coordinates).
+// kernel: differences are formed from hi/lo split coordinates).  rotn =
+// (x - y).n for the double-layer kernels (dot_dn), unused otherwise.
 template <int OP, bool MASK = true>
-__device__ __forceinline__ void eval_f32(float dx, float dy, float dz, float gx, float gy,
-                                         float gz, float kappa, float& kr, float& ki) {
+__device__ __forceinline__ void eval_f32(float dx, float dy, float dz, float rotn, float kappa, float& kr,
+                                         float& ki) {
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   if constexpr (OP == SKF_LAPLACE_2D) {
     // log r = (ln 2 / 2) * log2(r^2)
@@ -176,7 +211,6 @@ __device__ __forceinline__ void eval_f32(float dx, float dy, float dz, float gx,
     if (!MASK || r2 > 0.f) {
       const float ir = rsqrt_approx(r2);
       const float ir3 = ir * ir * ir;
-      const float rotn = dx * gx + dy * gy + dz * gz;
       if constexpr (OP == SKF_LAPLACE_DOUBLE_LAYER_3D) {
         kr = -float(kInv4Pi) * rotn * ir3;
         ki = 0.f;

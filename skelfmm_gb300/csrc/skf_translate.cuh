@@ -182,10 +182,11 @@ __global__ void __launch_bounds__(kTransThreads) k_translate_f64(TransArgs a) {
 // pair), which keeps the FP64 pipe out of the loop.
 template <int OP, bool H, bool SELF, int RPT>
 __device__ __forceinline__ void t32_tile(const float4* __restrict__ sA, const float4* __restrict__ sB,
-                                         const float4* __restrict__ sC, const float* __restrict__ sD, int nt,
-                                         const float4 (&th)[RPT], const float4 (&tl)[RPT], const float4 (&tg)[RPT],
-                                         float kappa, float (&pur)[RPT], float (&pui)[RPT], float (&phr)[RPT],
-                                         float (&phi)[RPT]) {
+                                         const float4* __restrict__ sC, const float* __restrict__ sD,
+                                         const float4* __restrict__ sE, int nt, const float4 (&th)[RPT],
+                                         const float4 (&tl)[RPT], const float4 (&tg)[RPT],
+                                         const float4 (&tgl)[RPT], float kappa, float (&pur)[RPT],
+                                         float (&pui)[RPT], float (&phr)[RPT], float (&phi)[RPT]) {
   constexpr bool C = OpTraits<OP>::kComplex;
   constexpr int G = OpTraits<OP>::kGeom;
 #pragma unroll 4
@@ -194,24 +195,23 @@ __device__ __forceinline__ void t32_tile(const float4* __restrict__ sA, const fl
     float4 Cc = make_float4(0, 0, 0, 0);
     if (C || G == 1) Cc = sC[j];
     float gzs = 0;
-    if (G == 1) gzs = sD[j];
+    float4 gl = make_float4(0, 0, 0, 0);
+    if (G == 1) {
+      gzs = sD[j];
+      gl = sE[j];
+    }
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
-      const float dx = (th[k].x - A.x) + (tl[k].x - B.x);
-      const float dy = (th[k].y - A.y) + (tl[k].y - B.y);
-      const float dz = (th[k].z - A.z) + (tl[k].z - B.z);
-      float gx = 0, gy = 0, gz = 0;
-      if (G == 1) {
-        gx = Cc.z;
-        gy = Cc.w;
-        gz = gzs;
-      } else if (G == 2) {
-        gx = tg[k].x;
-        gy = tg[k].y;
-        gz = tg[k].z;
-      }
+      const float dhx = th[k].x - A.x, dlx = tl[k].x - B.x;
+      const float dhy = th[k].y - A.y, dly = tl[k].y - B.y;
+      const float dhz = th[k].z - A.z, dlz = tl[k].z - B.z;
+      const float dx = dhx + dlx, dy = dhy + dly, dz = dhz + dlz;
+      float rotn = 0.f;
+      if (G == 1) rotn = dot_dn(dhx, dhy, dhz, dlx, dly, dlz, Cc.z, Cc.w, gzs, gl.x, gl.y, gl.z);
+      else if (G == 2)
+        rotn = dot_dn(dhx, dhy, dhz, dlx, dly, dlz, tg[k].x, tg[k].y, tg[k].z, tgl[k].x, tgl[k].y, tgl[k].z);
       float kr, ki;
-      eval_f32<OP, SELF>(dx, dy, dz, gx, gy, gz, kappa, kr, ki);
+      eval_f32<OP, SELF>(dx, dy, dz, rotn, kappa, kr, ki);
       if (C) {
         pur[k] = fmaf(kr, A.w, fmaf(-ki, Cc.x, pur[k]));
         pui[k] = fmaf(kr, Cc.x, fmaf(ki, A.w, pui[k]));
@@ -246,6 +246,7 @@ struct TransArgs32 {
   const float4* hi32;
   const float4* lo32;
   const float4* geom32;
+  const float4* geom32lo;
   const float* q32;
   const float* qhn32;
   const float* qd32;
@@ -265,6 +266,7 @@ __global__ void __launch_bounds__(kT32Threads) k_translate_f32(TransArgs32 a) {
   __shared__ float4 sB[TS];  // lx, ly, lz, c2r
   __shared__ float4 sC[(C || G == 1) ? TS : 1];  // c1i, c2i, gx, gy
   __shared__ float sD[(G == 1) ? TS : 1];        // gz
+  __shared__ float4 sE[(G == 1) ? TS : 1];       // lo parts of the normal
 
   const int U = a.work_box[blockIdx.x];
   const int row0 = a.work_row[blockIdx.x];
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(kT32Threads) k_translate_f32(TransArgs32 a) {
   const int rU = a.box_rank[U];
   const int rowt = row0 + RPT * threadIdx.x;  // first row of this thread
 
-  float4 th[RPT], tl[RPT], tg[RPT];
+  float4 th[RPT], tl[RPT], tg[RPT], tgl[RPT];
 #pragma unroll
   for (int k = 0; k < RPT; ++k) {
     const int row = rowt + k;
@@ -281,6 +283,7 @@ __global__ void __launch_bounds__(kT32Threads) k_translate_f32(TransArgs32 a) {
     th[k] = a.hi32[e];
     tl[k] = a.lo32[e];
     tg[k] = (G == 2) ? a.geom32[e] : make_float4(0, 0, 0, 0);
+    tgl[k] = (G == 2) ? a.geom32lo[e] : make_float4(0, 0, 0, 0);
   }
   // skeleton rows need uh; decided per warp so the branch stays uniform
   const bool need_h = (row0 + RPT * (threadIdx.x & ~31)) < rU;
@@ -322,7 +325,10 @@ __global__ void __launch_bounds__(kT32Threads) k_translate_f32(TransArgs32 a) {
         if (C || G == 1) {
           const float4 g = (G == 1) ? a.geom32[e] : make_float4(0, 0, 0, 0);
           sC[j] = make_float4(c1i, c2i, g.x, g.y);
-          if (G == 1) sD[j] = g.z;
+          if (G == 1) {
+            sD[j] = g.z;
+            sE[j] = a.geom32lo[e];
+          }
         }
       }
       __syncthreads();
@@ -331,11 +337,11 @@ __global__ void __launch_bounds__(kT32Threads) k_translate_f32(TransArgs32 a) {
       for (int k = 0; k < RPT; ++k) pur[k] = pui[k] = phr[k] = phi[k] = 0.f;
       const bool doh = need_h && hseg;
       if (doh) {
-        if (self) t32_tile<OP, true, true, RPT>(sA, sB, sC, sD, nt, th, tl, tg, a.kappa, pur, pui, phr, phi);
-        else t32_tile<OP, true, false, RPT>(sA, sB, sC, sD, nt, th, tl, tg, a.kappa, pur, pui, phr, phi);
+        if (self) t32_tile<OP, true, true, RPT>(sA, sB, sC, sD, sE, nt, th, tl, tg, tgl, a.kappa, pur, pui, phr, phi);
+        else t32_tile<OP, true, false, RPT>(sA, sB, sC, sD, sE, nt, th, tl, tg, tgl, a.kappa, pur, pui, phr, phi);
       } else {
-        if (self) t32_tile<OP, false, true, RPT>(sA, sB, sC, sD, nt, th, tl, tg, a.kappa, pur, pui, phr, phi);
-        else t32_tile<OP, false, false, RPT>(sA, sB, sC, sD, nt, th, tl, tg, a.kappa, pur, pui, phr, phi);
+        if (self) t32_tile<OP, false, true, RPT>(sA, sB, sC, sD, sE, nt, th, tl, tg, tgl, a.kappa, pur, pui, phr, phi);
+        else t32_tile<OP, false, false, RPT>(sA, sB, sC, sD, sE, nt, th, tl, tg, tgl, a.kappa, pur, pui, phr, phi);
       }
 #pragma unroll
       for (int k = 0; k < RPT; ++k) {

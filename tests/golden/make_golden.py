@@ -1,9 +1,10 @@
 """Generate the golden fixtures in this folder by running the reference
 implementation (annayesy/skelFMM, pure Python) on small seeded inputs.
 
-Run from the repository root, with the reference checkout available:
+Run from the repository root with the path of a reference checkout
+(optionally followed by the names of the build cases to regenerate):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference-checkout> [case ...]
 
 The reference imports the external ``simpletree`` package, which is not
 vendored; ``simpletree_shim/`` stands in for it with the framework's own tree,
@@ -48,18 +49,45 @@ CASES = [
     ("lapadl3d_sphere", "LAPLACE_ADJOINT_DOUBLE_LAYER_3D", "sphere_surface", 1500, 40, 1e-5, 0.0, 200, 7),
     ("helmdl3d_sphere", "HELMHOLTZ_DOUBLE_LAYER_3D", "sphere_surface", 1500, 40, 1e-5, 2.0, 200, 8),
     ("helmadl3d_sphere", "HELMHOLTZ_ADJOINT_DOUBLE_LAYER_3D", "sphere_surface", 1500, 40, 1e-5, 2.0, 200, 9),
+    # The benchmark's parameters (3D Laplace, tol 1e-6, leaf 400: 512 proxy
+    # points): a sparse cube with two dense neighbouring level-3 boxes, so the
+    # tree has a skeletonized level of parent boxes with 1,000+ entries.
+    ("lap3d_c2params", "LAPLACE_3D", "cube_two_dense_boxes", 9202, 400, 1e-6, 0.0, 500, 10),
+    # 3D Helmholtz on the sphere at tol 1e-6, leaf 400, kappa h_leaf = 1.25.
+    ("helm3d_sphere_k5", "HELMHOLTZ_3D", "sphere_surface", 24000, 400, 1e-6, 5.0, 500, 11),
+    # double layers at tol 1e-6
+    ("lapdl3d_sphere_1e6", "LAPLACE_DOUBLE_LAYER_3D", "sphere_surface", 2000, 40, 1e-6, 0.0, 200, 12),
+    ("helmdl3d_sphere_1e6", "HELMHOLTZ_DOUBLE_LAYER_3D", "sphere_surface", 2000, 40, 1e-6, 2.0, 200, 13),
 ]
 
 
-def make_builds():
+def _points(geom_name, N, rng):
+    from simpletree import get_point_dist
+
+    if geom_name == "cube_two_dense_boxes":
+        # two corners pin the root box to [0,1]^3; 3000 uniform points; 3100
+        # points uniform in each of the level-3 boxes [3/8,1/2]^3 and
+        # [1/2,5/8]x[3/8,1/2]^2 (8 leaves of ~390 points each)
+        ncl = (N - 3002) // 2
+        bg = rng.random((3000, 3))
+        c1 = 0.377 + rng.random((ncl, 3)) * 0.121
+        c2 = 0.377 + rng.random((N - 3002 - ncl, 3)) * 0.121
+        c2[:, 0] += 0.125
+        return np.vstack([np.array([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0]]), bg, c1, c2])
+    return get_point_dist(N, geom_name, rng=rng)
+
+
+def make_builds(only=()):
     import torch
     from skelfmm import RecursiveSkeletonization, SkelFMMBatched, operators
-    from simpletree import BalancedTree, get_point_dist
+    from simpletree import BalancedTree
 
     for name, opname, geom_name, N, leaf, tol, kappa, npmax, seed in CASES:
+        if only and name not in only:
+            continue
         op = getattr(operators, opname)
         rng = np.random.default_rng(seed)
-        pts = get_point_dist(N, geom_name, rng=rng)
+        pts = _points(geom_name, N, rng)
         geometry = None
         if op.requires_geometry:
             geometry = pts / np.linalg.norm(pts, axis=1, keepdims=True)
@@ -217,8 +245,11 @@ def make_ids():
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    _setup_paths(ref)
-    make_kernels()
-    make_ids()
-    make_builds()
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <reference-checkout> [case ...]")
+    _setup_paths(sys.argv[1])
+    only = tuple(sys.argv[2:])
+    if not only:
+        make_kernels()
+        make_ids()
+    make_builds(only)

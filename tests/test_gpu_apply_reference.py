@@ -44,10 +44,11 @@ def test_mixed_apply_meets_tolerance(name):
     d, plan = _plan(name)
     y = np.empty_like(d["x"])
     plan.apply_host(np.ascontiguousarray(d["x"]), y, _lib.PREC_MIXED)
-    # mixed = FP32 kernel evaluation on top of the FMM's own approximation.
-    # Double-layer kernels lose more: (x-y).n cancels for points on a surface
-    # (|(x-y).n| ~ r^2), so FP32 rounding of x-y costs ~1e-7/r relatively.
-    tol = 1e-4 if "DOUBLE_LAYER" in str(d["operator"]) else 2e-6
+    # mixed = FP32 kernel evaluation on top of the FMM's own approximation;
+    # the same bound for every operator (the double layers' (x-y).n, which
+    # cancels to ~r^2 on a surface, is formed from FP32 pairs to FP32
+    # rounding of the result)
+    tol = 2e-6
     err_fmm = relinf(d["y_batched"][d["dense_idx"]], d["y_dense"])
     assert relinf(y, d["y_batched"]) < tol
     assert relinf(y[d["dense_idx"]], d["y_dense"]) < err_fmm + tol

@@ -38,5 +38,7 @@ def test_kernel_blocks_match_reference(precision):
         if precision == 0:
             tol = 1e-9 if kname == "helmholtz_2d" else 1e-10
         else:
-            tol = 5e-5 if "double_layer" in kname else 2e-6
+            # double layers included: (x-y).n is formed to FP32 rounding of
+            # the result (compensated dot product of FP32 pairs)
+            tol = 2e-6
         assert relinf(out, g["out"]) < tol, (key, relinf(out, g["out"]))
