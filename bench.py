@@ -14,7 +14,12 @@ device-resident throughput (inputs in HBM, CUDA events on the launch stream);
 Multi-GPU runs are independent replicas (one instance per rank, no
 collective on the data path); ``value`` sums all ranks.
 ``--impl reference`` times the reference algorithm's CPU implementation (the
-oracle port of skelfmm's batched apply) on the host cores.
+oracle port of skelfmm's batched apply) on all host cores, on the same config:
+complete applies when they are short, otherwise each step times a random
+sample of the apply's kernel blocks (drawn in proportion to their work) and
+the apply time is estimated from the sampled rate; the estimate is checked
+against a complete apply (``calibration``).  The GPU arm's ``cpu_baseline``
+uses the same estimator.
 
 Other workloads (``--workload``): ``laplace2d_square_100k`` (2D Laplace,
 N = 1e5 uniform in [0,1]^2, tol 1e-5, leaf 200), ``helmholtz3d_sphere_2M``
@@ -37,7 +42,13 @@ import sys
 import threading
 import time
 
-import numpy as np
+# The reference arm (and the GPU arm's cpu_baseline) evaluates kernel blocks
+# on every host core through a thread pool; one BLAS thread per pool thread
+# keeps the cores from being oversubscribed.  Read by numpy's BLAS at import.
+for _v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+    os.environ.setdefault(_v, "1")
+
+import numpy as np  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
@@ -83,6 +94,26 @@ def single_config(args):
     leaf = args.leaf or leaf
     desc = f"{opname} {geo} N={n:.0e} tol={tol:g} leaf={leaf}" + (f" kappa={kappa:g}" if kappa else "")
     return dict(op=op, opname=opname, geo=geo, n=n, tol=tol, leaf=leaf, kappa=kappa, cplx=cplx, desc=desc)
+
+
+L2_NOTE = "GPU arm: 256 MB buffer zeroed between timed steps (outside the step events)"
+
+
+def single_config_dict(cfg, ngpus):
+    """The workload's config, printed identically by both arms."""
+    return {"workload": cfg["desc"], "N": cfg["n"], "tol": cfg["tol"], "leaf_size": cfg["leaf"],
+            "kappa": cfg["kappa"], "points": f"{cfg['geo']}, numpy default_rng(rank)",
+            "charges": "RandomState(1).randn" + (" + 1j RandomState(2).randn" if cfg["cplx"] else ""),
+            "l2": L2_NOTE, "parallelism": f"replicas x{ngpus}"}
+
+
+BATCH_CFG = dict(opname="laplace_2d", kappa=0.0, tol=1e-6, leaf=128, geo="curvy_annulus", cplx=False)
+
+
+def batch_config_dict(ntot, ninst, ngpus):
+    return {"workload": "64 x laplace_2d curvy annulus, N log-uniform [1e3, 2e5] (default_rng(rank)), "
+                        "tol=1e-6 leaf=128", "N_total": int(ntot), "instances": int(ninst), "l2": L2_NOTE,
+            "parallelism": f"replicas x{ngpus}"}
 
 
 def workload(cfg, seed=0):
@@ -190,38 +221,148 @@ def reduce_over_ranks(dist, value, op, device):
     return float(t.item())
 
 
-def cpu_baseline_sample(rb, x, opname="laplace_3d", kappa=0.0, budget_s=15.0):
-    """Reference algorithm (oracle port: FP64 dense kernel blocks) on the host
-    cores, over a sample of target boxes of the same ragged build; throughput
-    scaled by pair evaluations."""
-    from oracle import skel_oracle as O
+class ReferenceApply:
+    """The reference algorithm's FP64 CPU apply (the oracle port of
+    skelfmm's batched apply, skelfmm/batched_fmm.py:382-564) over one or more
+    built instances, on all host threads, timed in full or on a bounded
+    sample.
 
-    nb = rb.nboxes
-    rng = np.random.default_rng(0)
-    order = rng.permutation(nb)
-    work = np.array([(rb.box_off[b + 1] - rb.box_off[b]) *
-                     sum(rb.box_off[s + 1] - rb.box_off[s] for s in rb.list_src[rb.list_off[b]:rb.list_off[b + 1]])
-                     for b in range(nb)], dtype=np.float64)
-    total = float(work.sum())
-    q = np.zeros(rb.nentries, dtype=np.asarray(x).dtype)
-    q[rb.perm_entry] = x[rb.perm_point]
-    qh = q.copy()
-    nthreads = os.cpu_count() or 1
-    done_pairs, secs, i = 0, 0.0, 0
-    while secs < budget_s and i < nb:
-        chunk = [b for b in order[i:i + 4 * nthreads] if work[b] > 0]
-        i += 4 * nthreads
+    ``full()`` times complete applies.  ``sampled()`` times the upward and
+    downward passes in full and, per step, a random set of the apply's kernel
+    blocks drawn with probability proportional to their evaluations (a
+    step's mix of block sizes is the apply's), largest first; the apply time
+    is then the passes plus all evaluations over the sampled rate.  Both
+    arms of the benchmark use this one estimator."""
+
+    def __init__(self, builds, xs, ncores):
+        from oracle import skel_oracle as O
+
+        self.ncores = ncores
+        self.inst = []
+        self.items, self.cost = [], []
+        for k, (ob, x) in enumerate(zip(builds, xs)):
+            oa = O.OracleApply(ob, nthreads=ncores)
+            self.inst.append((oa, np.asarray(x)))
+            for u, s_, kind, c in oa.work_items():
+                self.items.append((k, u, s_, kind))
+                self.cost.append(c)
+        self.cost = np.asarray(self.cost, dtype=np.float64)
+        self.total = float(self.cost.sum())
+        self.npoints = int(sum(x.shape[0] for _, x in self.inst))
+
+    def full(self):
         t0 = time.perf_counter()
-        res = O.translation_sample(opname, kappa, rb.entry_xyz, None, rb.box_off, rb.box_rank,
-                                   rb.list_off, rb.list_src, rb.list_kind, q, qh, chunk, nthreads)
-        secs += time.perf_counter() - t0
-        done_pairs += sum(r[2] for r in res)
-    rate = done_pairs / secs
-    t_apply = total / rate
-    return {"value": rb.npoints / t_apply / 1e6, "unit": "Mpts/s", "cores": nthreads, "kind": "port",
-            "sample": f"{done_pairs:.3g} of {total:.3g} kernel evaluations ({100 * done_pairs / total:.2f}%) "
-                      f"in {secs:.1f} s, FP64 numpy dense blocks, {nthreads} threads; apply time scaled by "
-                      f"evaluation count"}
+        for oa, x in self.inst:
+            oa.matvec(x)
+        return time.perf_counter() - t0
+
+    def sampled(self, steps, warmup, step_evals, seed=0):
+        t0 = time.perf_counter()
+        qs = [oa.upward(x) for oa, x in self.inst]
+        t_up = time.perf_counter() - t0
+        p = self.cost / self.total
+        per_item = float((self.cost * p).sum())  # expected evaluations of one draw
+        # at least 8 blocks per thread, so the last blocks of a step (the
+        # threads' uneven finish) stay a small part of it
+        k = max(8 * self.ncores, int(np.ceil(step_evals / per_item)))
+        rng = np.random.default_rng(seed)
+
+        def step():
+            sel = rng.choice(len(self.items), size=k, p=p)
+            sel = sel[np.argsort(-self.cost[sel], kind="stable")]  # largest blocks first
+            by_inst = {}
+            for i in sel:
+                it = self.items[i]
+                by_inst.setdefault(it[0], []).append(it[1:])
+            t = time.perf_counter()
+            done = sum(self.inst[j][0].translate_items(lst, *qs[j]) for j, lst in by_inst.items())
+            return done, time.perf_counter() - t
+
+        for _ in range(warmup):
+            step()
+        done, secs, per = 0, 0.0, []
+        for _ in range(steps):
+            d_, s_ = step()
+            done += d_
+            secs += s_
+            per.append(s_)
+        t0 = time.perf_counter()
+        for (oa, x), (q, qh) in zip(self.inst, qs):
+            oa.downward([np.zeros_like(v) for v in q], [np.zeros_like(v) for v in q], x.shape)
+        t_down = time.perf_counter() - t0
+        rate = done / secs
+        t_apply = t_up + self.total / rate + t_down
+        return {"apply_s": t_apply, "rate_evals_per_s": rate, "sampled_evals": done, "sample_s": secs,
+                "step_evals": done / max(steps, 1), "blocks_per_step": k,
+                "step_s": float(np.mean(per)), "up_s": t_up, "down_s": t_down, "evals_per_apply": self.total}
+
+
+def oracle_builds(point_sets, opname, kappa, tol, leaf, ncores):
+    """Oracle builds (the reference's pivoted-QR build restated) of the point
+    sets, on a spawn pool with one BLAS thread per worker."""
+    from oracle import skel_oracle as O
+    from skelfmm_gb300.tree import BalancedTree
+
+    out = []
+    with oracle_pool(ncores) as pool:
+        for pts in point_sets:
+            tree = BalancedTree(pts, leaf)
+            out.append(O.OracleBuild(tree, O.OPERATORS[opname], kappa, tol).skel_tree(500, pool=pool))
+    return out
+
+
+# evaluations per sampled step of the reference arm (at least 8 blocks per thread)
+REF_STEP_EVALS = 1.5e8
+# size of the calibration instance of a workload (a complete apply in ~15 s on 16 cores)
+CAL_N = {"cube": 100_000, "sphere_surface": 100_000, "square": 100_000}
+
+
+def reference_baseline(cfg, point_sets, xs, ncores, steps, warmup, calibrate=True):
+    """The reference algorithm on the host cores for a workload: complete
+    applies when they are short, otherwise the sampled estimate, checked
+    against a complete apply (of the workload itself when one is short, else
+    of a smaller instance of the same workload)."""
+    t0 = time.perf_counter()
+    builds = oracle_builds(point_sets, cfg["opname"], cfg["kappa"], cfg["tol"], cfg["leaf"], ncores)
+    build_s = time.perf_counter() - t0
+    ra = ReferenceApply(builds, xs, ncores)
+    probe = ra.sampled(1, 0, REF_STEP_EVALS)
+    out = {"build_s": build_s, "npoints": ra.npoints, "evals_per_apply": ra.total}
+    if probe["apply_s"] * (steps + warmup) < 90.0:
+        for _ in range(warmup):
+            ra.full()
+        per = [ra.full() for _ in range(steps)]
+        out.update(kind="complete", apply_s=float(np.mean(per)), step_s=float(np.mean(per)),
+                   sample=f"{steps} complete applies, FP64 numpy dense kernel blocks")
+        return out
+    est = ra.sampled(steps, warmup, REF_STEP_EVALS)
+    if calibrate and probe["apply_s"] < 60.0:
+        t_full = ra.full()
+        out["calibration"] = {"N": ra.npoints, "complete_apply_s": round(t_full, 3),
+                              "sampled_estimate_s": round(est["apply_s"], 3),
+                              "estimate_over_complete": round(est["apply_s"] / t_full, 3)}
+    elif calibrate:
+        out["calibration"] = reference_calibration(cfg, ncores)
+    out.update(kind="sampled", apply_s=est["apply_s"], step_s=est["step_s"],
+               sample=f"{steps} steps x {est['blocks_per_step']} kernel blocks (~{est['step_evals']:.2g} "
+                      f"evaluations) drawn in proportion to the apply's blocks, largest first "
+                      f"({100 * est['sampled_evals'] / ra.total:.2f}% of one apply in all), "
+                      f"FP64 numpy dense kernel blocks; apply time = upward + downward passes "
+                      f"({est['up_s'] + est['down_s']:.2f} s, timed in full) + evaluations / sampled rate")
+    return out
+
+
+def reference_calibration(cfg, ncores):
+    """The sampled estimate against a complete apply, both on a smaller
+    instance of the workload (same operator, tol and leaf size)."""
+    small = dict(cfg, n=CAL_N.get(cfg["geo"], 100_000))
+    pts, x = workload(small)
+    builds = oracle_builds([pts], small["opname"], small["kappa"], small["tol"], small["leaf"], ncores)
+    ra = ReferenceApply(builds, [x], ncores)
+    t_full = ra.full()
+    est = ra.sampled(5, 1, REF_STEP_EVALS)
+    return {"N": small["n"], "complete_apply_s": round(t_full, 3), "sampled_estimate_s": round(est["apply_s"], 3),
+            "estimate_over_complete": round(est["apply_s"] / t_full, 3)}
 
 
 # FP32 FMA-pipe ops per kernel evaluation in the algorithm: D subtractions and
@@ -354,18 +495,17 @@ def run_single(args):
     roofline = roofline_line(plan, t_ms, cfg["opname"], TRAFFIC_PROFILE.get(args.workload, ""))
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(plan.rb, x, cfg["opname"], cfg["kappa"])
+        ncores = os.cpu_count() or 1
+        res = reference_baseline(cfg, [pts], [x], ncores, steps=4, warmup=1, calibrate=False)
+        cpu = {"value": round(res["npoints"] / res["apply_s"] / 1e6, 6), "unit": "Mpts/s", "cores": ncores,
+               "kind": "port", "sample": res["sample"]}
     value = n * ws / (ms_step * 1e-3) / 1e6
     line = {
         "metric": METRIC[args.workload],
         "value": round(value, 2), "unit": "Mpts/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 kernel eval, f64 accumulation" + (", complex" if cfg["cplx"] else ""), "data": "synthetic",
-        "config": {"workload": cfg["desc"], "N": n, "tol": cfg["tol"], "leaf_size": cfg["leaf"],
-                   "kappa": cfg["kappa"], "points": f"{cfg['geo']}, numpy default_rng(rank)",
-                   "charges": "RandomState(1).randn" + (" + 1j RandomState(2).randn" if cfg["cplx"] else ""),
-                   "l2": "256 MB buffer zeroed between timed steps (outside the step events)",
-                   "parallelism": f"replicas x{ws}"},
+        "config": single_config_dict(cfg, ws),
         "e2e": {"value": round(n * ws / e2e_s / 1e6, 2), "unit": "Mpts/s", "h2d_bytes_per_step": n * 8 * W,
                 "d2h_bytes_per_step": n * 8 * W, "ms_per_step": round(e2e_s * 1e3, 3)},
         "gpu_launches": int(plan.info.launches_mixed) * args.steps,
@@ -456,7 +596,10 @@ def run_batch(args):
     roofline = roofline_line(b.plan, t_ms, "laplace_2d", "")
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(b.plan.rb, np.concatenate(xs), "laplace_2d", 0.0)
+        ncores = os.cpu_count() or 1
+        res = reference_baseline(BATCH_CFG, pts, xs, ncores, steps=4, warmup=1, calibrate=False)
+        cpu = {"value": round(res["npoints"] / res["apply_s"] / 1e6, 6), "unit": "Mpts/s", "cores": ncores,
+               "kind": "port", "sample": res["sample"]}
     # ranks hold different instances: the job's units are summed over ranks
     nall = reduce_over_ranks(dist, ntot, "sum", dev)
     value = nall / (ms_step * 1e-3) / 1e6
@@ -464,11 +607,8 @@ def run_batch(args):
         "metric": METRIC["batch64_annulus"], "value": round(value, 2), "unit": "Mpts/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 kernel eval, f64 accumulation", "data": "synthetic",
-        "config": {"workload": "64 x laplace_2d curvy annulus, N log-uniform [1e3, 2e5] (default_rng(rank)), "
-                               "tol=1e-6 leaf=128", "N_total": ntot, "instances": len(pts),
-                   "tuned_scheme": {"symmetric": int(b.plan.tuned[0]), "packed_shape": int(b.plan.tuned[1])},
-                   "l2": "256 MB buffer zeroed between timed steps (outside the step events)",
-                   "parallelism": f"replicas x{ws}"},
+        "config": batch_config_dict(ntot, len(pts), ws),
+        "tuned_scheme": {"symmetric": int(b.plan.tuned[0]), "packed_shape": int(b.plan.tuned[1])},
         "e2e": {"value": round(nall / e2e_s / 1e6, 2), "unit": "Mpts/s", "h2d_bytes_per_step": ntot * 8,
                 "d2h_bytes_per_step": ntot * 8, "ms_per_step": round(e2e_s * 1e3, 3)},
         "gpu_launches": int(b.plan.info.launches_mixed) * args.steps,
@@ -559,36 +699,6 @@ def run_clusters(args):
         print(json.dumps(line), flush=True)
 
 
-def oracle_ragged(ob, tree):
-    """Ragged view (entry coordinates, offsets, per-target lists) of an oracle
-    build, for sampled CPU translations."""
-    nb = ob.nboxes
-    bs = ob.bs_list
-    off = np.zeros(nb + 1, dtype=np.int64)
-    np.cumsum(bs, out=off[1:])
-    xyz = np.concatenate([tree.XX[ob.pid[b]] for b in range(nb) if bs[b] > 0])
-    work = {}
-    for u, s_ in np.vstack((ob.leaf_uskel_from_qskel_list, ob.tree_uskel_from_qskel_list)):
-        work.setdefault(int(u), []).append((int(s_), 0))
-    for u, s_ in ob.uskel_from_q_list:
-        work.setdefault(int(u), []).append((int(s_), 1))
-    for u, s_ in ob.u_from_qskel_list:
-        work.setdefault(int(u), []).append((int(s_), 2))
-    for u, s_ in ob.u_from_q_list:
-        work.setdefault(int(u), []).append((int(s_), 3))
-    lo = np.zeros(nb + 1, dtype=np.int64)
-    srcs, kinds = [], []
-    for b in range(nb):
-        lst = work.get(b, [])
-        lo[b + 1] = lo[b] + len(lst)
-        srcs += [s_ for s_, _ in lst]
-        kinds += [k for _, k in lst]
-    srcs = np.array(srcs, dtype=np.int64)
-    kinds = np.array(kinds, dtype=np.int64)
-    wcost = np.array([bs[b] * sum(bs[s_] for s_ in srcs[lo[b]:lo[b + 1]]) for b in range(nb)], dtype=np.float64)
-    return xyz, off, lo, srcs, kinds, wcost
-
-
 def oracle_pool(ncores):
     """Spawn pool with one BLAS thread per worker (the workers read these at
     import; a multi-threaded BLAS in every worker oversubscribes the cores)."""
@@ -609,7 +719,9 @@ def oracle_pool(ncores):
 
 
 def run_reference(args):
-    """The reference algorithm on the host cores (oracle port), bounded sample per step."""
+    """The reference algorithm on the host cores (oracle port): complete
+    applies, or a bounded sample per step with a calibration (see
+    reference_baseline)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -619,85 +731,27 @@ def run_reference(args):
                           "takes tens of minutes, the pivoted-QR GPU build is this workload's baseline"}),
               flush=True)
         return
-    from oracle import skel_oracle as O
-    from skelfmm_gb300.tree import BalancedTree
-
     ncores = os.cpu_count() or 1
-    t0 = time.perf_counter()
     if args.workload == "batch64_annulus":
         pts_l, xs = batch_instances()
-        opname, kappa, tol, leaf = "laplace_2d", 0.0, 1e-6, 128
-        desc = "64 x laplace_2d curvy annulus, N log-uniform [1e3, 2e5], tol=1e-6 leaf=128"
+        cfg = BATCH_CFG
+        config = batch_config_dict(sum(p_.shape[0] for p_ in pts_l), len(pts_l), args.gpus)
     else:
         cfg = single_config(args)
         p_, x_ = workload(cfg)
         pts_l, xs = [p_], [x_]
-        opname, kappa, tol, leaf = cfg["opname"], cfg["kappa"], cfg["tol"], cfg["leaf"]
-        desc = cfg["desc"]
-    insts = []
-    with oracle_pool(ncores) as pool:
-        for pts, x in zip(pts_l, xs):
-            tree = BalancedTree(pts, leaf)
-            ob = O.OracleBuild(tree, O.OPERATORS[opname], kappa, tol).skel_tree(500, pool=pool)
-            insts.append((tree, ob, x))
-    build_s = time.perf_counter() - t0
-    data, t_up, total, n = [], 0.0, 0.0, 0
-    for tree, ob, x in insts:
-        xyz, off, lo, srcs, kinds, wcost = oracle_ragged(ob, tree)
-        oa = O.OracleApply(ob, nthreads=ncores)
-        t1 = time.perf_counter()
-        qv, qhv = oa.upward(x)
-        t_up += time.perf_counter() - t1
-        bs = ob.bs_list
-        q = np.concatenate([qv[b] for b in range(ob.nboxes) if bs[b] > 0])
-        qh = np.concatenate([qhv[b] for b in range(ob.nboxes) if bs[b] > 0])
-        data.append((xyz, off, ob.rank_list, lo, srcs, kinds, q, qh, wcost))
-        total += float(wcost.sum())
-        n += tree.N
-    rng = np.random.default_rng(0)
-    per_step = max(1e8, total / 200.0)
-    weights = np.array([d[-1].sum() for d in data])
-    weights = weights / weights.sum()
-
-    def step():
-        done, secs = 0, 0.0
-        while done < per_step:
-            i = int(rng.choice(len(data), p=weights))
-            xyz, off, rk, lo, srcs, kinds, q, qh, wcost = data[i]
-            nbx = wcost.shape[0]
-            sel, acc = [], 0.0
-            while acc < per_step / 4:
-                b = int(rng.integers(nbx))
-                if wcost[b] > 0:
-                    sel.append(b)
-                    acc += wcost[b]
-            t = time.perf_counter()
-            res = O.translation_sample(opname, kappa, xyz, None, off, rk, lo, srcs, kinds, q, qh, sel, ncores)
-            secs += time.perf_counter() - t
-            done += sum(r[2] for r in res)
-        return done, secs
-
-    for _ in range(args.warmup):
-        step()
-    pairs, secs = 0, 0.0
-    for _ in range(args.steps):
-        p_, s_ = step()
-        pairs += p_
-        secs += s_
-    rate = pairs / secs
-    t_apply = total / rate + 2 * t_up
-    value = n / t_apply / 1e6
+        config = single_config_dict(cfg, args.gpus)
+    res = reference_baseline(cfg, pts_l, xs, ncores, args.steps, args.warmup)
+    value = res["npoints"] / res["apply_s"] / 1e6
+    cpu = {"value": round(value, 6), "unit": "Mpts/s", "cores": ncores, "kind": "port", "sample": res["sample"]}
     line = {
-        "metric": METRIC[args.workload], "impl": "reference", "value": round(value, 4), "unit": "Mpts/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_apply * 1e3, 1),
+        "metric": METRIC[args.workload], "impl": "reference", "value": round(value, 6), "unit": "Mpts/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(res["step_s"] * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc, "N": n, "tol": tol, "leaf_size": leaf},
-        "build_s": round(build_s, 2),
-        "cpu_baseline": {"value": round(value, 4), "unit": "Mpts/s", "cores": ncores, "kind": "port",
-                         "sample": f"{args.steps} steps x ~{per_step:.3g} kernel evaluations of random target "
-                                   f"boxes ({100 * pairs / total:.2f}% of one apply), FP64 dense numpy blocks; "
-                                   f"apply time = evaluations / rate + upward/downward passes"},
-        "e2e": {"value": round(value, 4), "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": config, "apply_s": round(res["apply_s"], 3), "timing": res["kind"],
+        "evaluations_per_apply": res["evals_per_apply"], "build_s": round(res["build_s"], 2),
+        "calibration": res.get("calibration"), "cpu_baseline": cpu,
+        "e2e": {"value": round(value, 6), "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 

@@ -615,6 +615,39 @@ class OracleApply:
                 acc_u -= K[:, :rs] @ qh[s][:rs]
         return acc_u, acc_h
 
+    def work_items(self):
+        """Every kernel block of one apply as (target, source, kind, evaluations)."""
+        b = self.b
+        return [(u, s, kind, int(b.bs_list[u]) * int(b.bs_list[s]))
+                for u, lst in self.work.items() for s, kind in lst]
+
+    def translate_items(self, items, q, qh):
+        """The kernel blocks ``items`` (target, source, kind, ...) of one apply
+        with translate_box's arithmetic, spread over the host threads; returns
+        the kernel evaluations done.  Used to time a bounded sample of the
+        apply (the products are computed and dropped)."""
+        b = self.b
+
+        def one(it):
+            u, s, kind = int(it[0]), int(it[1]), int(it[2])
+            ru, rs = int(b.rank_list[u]), int(b.rank_list[s])
+            K = self._K(u, s)
+            acc_u = K @ q[s]
+            if kind == 0:
+                acc_h = -(K[:ru, :rs] @ qh[s][:rs])
+            elif kind == 1:
+                acc_h = -(K[:ru] @ q[s])
+            elif kind == 2:
+                acc_u = acc_u - K[:, :rs] @ qh[s][:rs]
+                acc_h = None
+            else:
+                acc_h = None
+            del acc_u, acc_h
+            return K.size
+
+        with ThreadPoolExecutor(self.nthreads) as ex:
+            return int(sum(ex.map(one, list(items))))
+
     def translations(self, q, qh, boxes=None):
         b = self.b
         boxes = list(self.work.keys()) if boxes is None else list(boxes)
