@@ -31,8 +31,8 @@ extern "C" {
 #define SKF_ERR_OOM 2         /* device allocation failed */
 #define SKF_ERR_CUDA 3        /* a CUDA runtime call failed */
 #define SKF_ERR_UNSUPPORTED 4 /* operator/precision combination not built */
-#define SKF_ERR_ID 5          /* interpolative decomposition failed (non-finite input) */
-#define SKF_ERR_TIMEOUT 6     /* a bounded device-side wait ran out */
+#define SKF_ERR_ID 5          /* interpolative decomposition failed: a proxy matrix has a
+                                 non-finite entry (a non-finite point or normal) */
 
 /* operators (skelfmm/operators.py:159-216) */
 #define SKF_LAPLACE_2D 0
@@ -173,10 +173,16 @@ int skf_skel_boxes(int32_t op, double kappa, int32_t nbox, const int64_t* off, c
  * workspace is a fixed file-scope device array of SKF_NOALLOC_SCRATCH_BYTES
  * that every GPU loading the library keeps until exit.  A box whose FP64
  * proxy matrix (rows x box size, x2 when complex) does not fit returns
- * SKF_ERR_SCRATCH before any work.  The first call on a device looks up the
- * array's address (cudaGetSymbolAddress) and should precede any stream
- * capture on that device.  All calls share the array: calls that overlap on
- * the GPU race and must be serialised by the caller.
+ * SKF_ERR_SCRATCH before any kernel launch or scratch write (the call first
+ * copies `off` to the host and synchronises `stream`, as skf_skel_boxes
+ * does).  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) and should precede any stream capture on that
+ * device; the address is kept for the process, so a cudaDeviceReset of that
+ * device invalidates it.  All calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller.  Every box runs on the
+ * 256-thread ID kernel (skf_skel_boxes moves its costliest boxes of 192+
+ * points to thread-block clusters), so for such boxes the redundant pivot
+ * order, decided at rounding level, can differ from skf_skel_boxes'.
  */
 #define SKF_NOALLOC_SCRATCH_BYTES (64ll << 20)
 #define SKF_ERR_SCRATCH 7 /* problem exceeds the fixed no-allocation scratch */

@@ -19,7 +19,6 @@ SKF_ERR_OOM = 2
 SKF_ERR_CUDA = 3
 SKF_ERR_UNSUPPORTED = 4
 SKF_ERR_ID = 5
-SKF_ERR_TIMEOUT = 6
 SKF_ERR_SCRATCH = 7
 
 PREC_FP64 = 0

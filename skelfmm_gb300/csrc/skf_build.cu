@@ -131,6 +131,9 @@ struct SkelArgs {
   // deferred fallback: a rejected randomized ID writes only its status and
   // residual; its pivoted-QR ID runs in a second launch over the rejects
   int defer;
+  // set to 1 by any block whose proxy matrix has a non-finite entry or whose
+  // points (normals) are not finite; NULL: unchecked
+  int* nonfinite;
 };
 
 constexpr int kSkelThreads = 256;
@@ -670,12 +673,19 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
       const double* xj = a.x + (off + j) * D;
       const double* gj = a.geom ? a.geom + (off + j) * 3 : nullptr;
       double* col = A + (int64_t)j * m * W;
+      // a non-finite point (or normal) would read as a zero column where
+      // the kernel masks r == 0, so the inputs are checked as well
+      bool bad = false;
+      for (int d = 0; d < D; ++d) bad |= !isfinite(xj[d]);
+      if (gj) bad |= !(isfinite(gj[0]) && isfinite(gj[1]) && isfinite(gj[2]));
       for (int i = lane; i < m; i += 32) {
         double kr, ki;
         proxy_entry<OP, RAND>(a, c, pts, i, xj, gj, kr, ki);
         col[i * W] = kr;
         if (C) col[i * W + 1] = ki;
+        bad |= !isfinite(kr) || (C && !isfinite(ki));
       }
+      if (bad && a.nonfinite) *a.nonfinite = 1;
     }
   }
   __syncthreads();
@@ -1064,11 +1074,16 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
     if (j >= n) continue;
     const double* xj = a.x + (off + j) * D;
     const double* gj = a.geom ? a.geom + (off + j) * 3 : nullptr;
+    bool bad = false;
+    for (int d = 0; d < D; ++d) bad |= !isfinite(xj[d]);
+    if (gj) bad |= !(isfinite(gj[0]) && isfinite(gj[1]) && isfinite(gj[2]));
     for (int i = lane; i < m; i += 32) {
       double kr, ki;
       proxy_entry<OP>(a, c, nullptr, i, xj, gj, kr, ki);
       A[(int64_t)j * m + i] = kr;
+      bad |= !isfinite(kr);
     }
+    if (bad && a.nonfinite) *a.nonfinite = 1;
   }
   __syncthreads();
 
@@ -1345,6 +1360,10 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     }
   }
 
+  int* dbad = nullptr;  // non-finite proxy entries seen by any block
+  SKF_CUDA_TRY(cudaMallocAsync(&dbad, sizeof(int), st));
+  SKF_CUDA_TRY(cudaMemsetAsync(dbad, 0, sizeof(int), st));
+
   // workspace in batches of boxes bounded by ~4 GiB
   const int64_t budget = (int64_t)4 << 30;
   int status = SKF_OK;
@@ -1417,6 +1436,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     a.nchk = ra.nchk;
     a.sketch_tol = ra.sketch_tol;
     a.resid_tol = ra.resid_tol;
+    a.nonfinite = dbad;
     int maxn_batch = 1;
     for (int b = b0; b < b1; ++b) maxn_batch = std::max<int>(maxn_batch, (int)(hoff[b + 1] - hoff[b]));
     // Launches the boxes `list` (batch-local) longest first; boxes far above
@@ -1499,6 +1519,18 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     cudaFreeAsync(dord, st);
     b0 = b1;
   }
+  if (status == SKF_OK) {
+    int bad = 0;
+    cudaError_t ce = cudaMemcpyAsync(&bad, dbad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) {
+      set_last_cuda_error(ce);
+      status = SKF_ERR_CUDA;
+    } else if (bad) {
+      status = SKF_ERR_ID;
+    }
+  }
+  cudaFreeAsync(dbad, st);
   cudaFreeAsync(dtmpl, st);
   if (dtab) cudaFreeAsync(dtab, st);
   if (own_stat) cudaFreeAsync(own_stat, st);
@@ -1542,7 +1574,8 @@ int skel_boxes_randomized(int op, double kappa, int nbox, const int64_t* off, co
 // offsets and the workspaces carved out of a caller-provided device buffer of
 // `cap` doubles instead of stream-ordered allocations.  Boxes are processed
 // in batches that fit the buffer, in stream order.  Returns SKF_ERR_SCRATCH,
-// before any device work, when one box's proxy matrix does not fit.
+// before any kernel launch or scratch write, when one box's proxy matrix does
+// not fit; SKF_ERR_ID when a proxy matrix (a point or normal) is not finite.
 int skel_boxes_scratch(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
                        const double* centers, double box_length, int nproxy, double tol, int32_t* rank,
                        int32_t* perm, const int64_t* t_off_out, void* t_out, double* scratch, int64_t cap,
@@ -1556,8 +1589,9 @@ int skel_boxes_scratch(int op, double kappa, int nbox, const int64_t* off, const
   const int np = (int)(tmpl.size() / ndim);
   const int mrows = geom_op ? 2 * np : np;
   constexpr int64_t kMaxBatch = 4096;  // workspace-offset slots
+  constexpr int64_t kFlagSlots = 32;   // the non-finite flag (one int in a 256-byte slot)
   const int64_t tsz = ((int64_t)tmpl.size() + 31) / 32 * 32;
-  const int64_t wcap = cap - tsz - kMaxBatch;
+  const int64_t wcap = cap - tsz - kMaxBatch - kFlagSlots;
   if (wcap <= 0) return SKF_ERR_SCRATCH;
   std::vector<int64_t> hoff(nbox + 1);
   SKF_CUDA_TRY(cudaMemcpyAsync(hoff.data(), off, sizeof(int64_t) * (nbox + 1), cudaMemcpyDeviceToHost, st));
@@ -1567,8 +1601,10 @@ int skel_boxes_scratch(int op, double kappa, int nbox, const int64_t* off, const
 
   double* dtmpl = scratch;
   int64_t* dwso = reinterpret_cast<int64_t*>(scratch + tsz);
-  double* ws = scratch + tsz + kMaxBatch;
+  int* dbad = reinterpret_cast<int*>(scratch + tsz + kMaxBatch);
+  double* ws = scratch + tsz + kMaxBatch + kFlagSlots;
   SKF_CUDA_TRY(cudaMemcpyAsync(dtmpl, tmpl.data(), sizeof(double) * tmpl.size(), cudaMemcpyHostToDevice, st));
+  SKF_CUDA_TRY(cudaMemsetAsync(dbad, 0, sizeof(int), st));
   int status = SKF_OK;
   int b0 = 0;
   while (b0 < nbox && status == SKF_OK) {
@@ -1603,6 +1639,7 @@ int skel_boxes_scratch(int op, double kappa, int nbox, const int64_t* off, const
     a.t_off_out = t_off_out;
     a.t_out = static_cast<double*>(t_out);
     a.first_box = b0;
+    a.nonfinite = dbad;
     int maxn_batch = 1;
     for (int b = b0; b < b1; ++b) maxn_batch = std::max<int>(maxn_batch, (int)(hoff[b + 1] - hoff[b]));
     switch (op) {
@@ -1620,6 +1657,12 @@ int skel_boxes_scratch(int op, double kappa, int nbox, const int64_t* off, const
       default: status = SKF_ERR_ARG;
     }
     b0 = b1;
+  }
+  if (status == SKF_OK) {
+    int bad = 0;
+    SKF_CUDA_TRY(cudaMemcpyAsync(&bad, dbad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SKF_CUDA_TRY(cudaStreamSynchronize(st));
+    if (bad) status = SKF_ERR_ID;
   }
   if (status == SKF_OK) SKF_CUDA_TRY(cudaGetLastError());
   return status;

@@ -109,7 +109,6 @@ const char* skf_status_string(int32_t s) {
     case SKF_ERR_CUDA: return g_last_where[0] ? g_last_where : cudaGetErrorString(g_last_cuda);
     case SKF_ERR_UNSUPPORTED: return "unsupported operator or precision";
     case SKF_ERR_ID: return "interpolative decomposition failed (non-finite proxy matrix)";
-    case SKF_ERR_TIMEOUT: return "device wait timed out";
     case SKF_ERR_SCRATCH: return "a box's proxy matrix exceeds the fixed no-allocation scratch (SKF_NOALLOC_SCRATCH_BYTES)";
     default: return "unknown status";
   }

@@ -17,10 +17,17 @@
 //   loads the library, for the life of the process.
 // * Boxes are processed in batches that fit; one box whose proxy matrix
 //   (rows x box size, x2 for complex kernels, FP64) does not fit beside the
-//   proxy template is rejected with SKF_ERR_SCRATCH before any device work.
+//   proxy template is rejected with SKF_ERR_SCRATCH before any kernel launch
+//   or scratch write (the call first copies `off` to the host and
+//   synchronises the stream).
 // * The first call on a device looks up the array's device address with
 //   cudaGetSymbolAddress while that device is current; make that first call
-//   before starting any stream capture on the device.
+//   before starting any stream capture on the device.  The address is kept
+//   for the life of the process: a cudaDeviceReset of the device invalidates
+//   it.
+// * Every box runs on the 256-thread ID kernel; skf_skel_boxes moves the
+//   costliest boxes of 192+ points to thread-block clusters, whose pivot order
+//   past the rank (decided at rounding level) can differ.
 // * Every call shares the array and it keeps the last call's contents.
 //   Nothing in it has to start at zero (each call writes everything it
 //   reads), but calls that overlap on the GPU (other streams, other host

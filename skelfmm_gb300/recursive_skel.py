@@ -96,6 +96,21 @@ class RecursiveSkeletonization:
 
         self.nproxy_level = nproxy_levels(self.ndim, tol, self.kappa, tree.L0, self.nlevels)
         self.max_bs_leaf = tree.leaf_size
+        # max_bs / max_rank size the reference's padded storage before the
+        # build (skelfmm/recursive_skel.py:87-94); it grows that storage when a
+        # box needs more (:230-247, :285-307), so they never cap a rank.  The
+        # ragged layout here has no padded storage: both are validated and
+        # kept as the reference computes them, and do not change the build.
+        for name, v in (("max_bs", max_bs), ("max_rank", max_rank)):
+            if int(v) != v:
+                raise ValueError(f"{name} must be an integer")
+        if max_bs > 0 and max_rank > 0:
+            self.max_rank = int(max_rank)
+            self.max_bs = max(int(max_bs), int(self.max_bs_leaf))
+        else:
+            self.max_rank = int(self.max_bs_leaf * 0.75)
+            self.max_bs = int((2 ** self.ndim) * self.max_bs_leaf)
+        self.max_rank_leaf = self.max_rank
         if np.any(tree.get_box_npoints(tree.get_leaves()) > self.max_bs_leaf):
             raise ValueError("Leaf block size exceeds maximum allowed")
         self.bs_list = np.zeros(self.nboxes, dtype=np.int64)

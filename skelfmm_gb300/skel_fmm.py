@@ -87,6 +87,10 @@ class SkelFMM:
                  use_single_precision=False, param=0.0, quiet=True, keep_host_fmm=False, defer_build=False,
                  npoints_max=500, p="auto", max_bs=-1, max_rank=-1, precision=None, learned_rank=False):
         self.points = np.asarray(points, dtype=np.float64)
+        if self.points.ndim != 2 or not np.all(np.isfinite(self.points)):
+            raise ValueError("points must be a finite [N, ndim] array")
+        if geometry is not None and not np.all(np.isfinite(np.asarray(geometry, dtype=np.float64))):
+            raise ValueError("geometry must be finite")
         # learned_rank: False (pivoted-QR IDs, as the reference), True (packaged
         # rank network), a path to weights, or a RankMLP
         self.learned_rank = learned_rank
@@ -109,8 +113,13 @@ class SkelFMM:
         self.precision = precision
         self._build_npoints_max = npoints_max
         self._build_p = p
-        self._max_bs_limit = max_bs
-        self._max_rank_limit = max_rank
+        for name, v in (("max_bs", max_bs), ("max_rank", max_rank)):
+            if int(v) != v:
+                raise ValueError(f"{name} must be an integer")
+        # pre-sizes of the reference's padded storage (never a rank cap there);
+        # passed to RecursiveSkeletonization, which reports them
+        self._max_bs_limit = int(max_bs)
+        self._max_rank_limit = int(max_rank)
         self._is_built = False
         self._lazy_build_notice_printed = False
 
@@ -207,6 +216,9 @@ class SkelFMM:
             raise ValueError("apply expects a 1D vector")
         if x_np.shape[0] != self.points.shape[0]:
             raise ValueError("Source vector length must match the number of points")
+        if not np.all(np.isfinite(x_np)):
+            # one non-finite charge reaches every output through the far field
+            raise ValueError("apply expects finite charges")
         cplx = is_complex_op(self.operator)
         if np.iscomplexobj(x_np) and not cplx:
             re = self.apply(np.ascontiguousarray(x_np.real))

@@ -79,3 +79,67 @@ def test_errors_map_to_python_exceptions():
     with pytest.raises(_lib.SkfError) as e:
         _lib.check(_lib.SKF_ERR_SCRATCH, "x")
     assert e.value.status == _lib.SKF_ERR_SCRATCH
+
+
+def test_non_finite_coordinates_are_rejected_by_plan_create(lib):
+    """A NaN coordinate in the ragged description: SKF_ERR_ARG before any
+    device allocation (the host validation runs first)."""
+    import numpy as np
+
+    from skelfmm_gb300 import _lib
+
+    xyz = np.array([[0.1, 0.2, 0.3], [np.nan, 0.5, 0.5]])
+    keep = dict(level=np.zeros(1, np.int32), off=np.array([0, 2], np.int64), rank=np.zeros(1, np.int32),
+                pslot=np.full(2, -1, np.int64), pe=np.arange(2, dtype=np.int64), pp=np.arange(2, dtype=np.int64),
+                toff=np.full(1, -1, np.int64), t=np.zeros(1), loff=np.array([0, 1], np.int64),
+                lsrc=np.zeros(1, np.int32), lkind=np.full(1, 3, np.int8), xyz=xyz)
+    d = _lib.PlanDesc()
+    d.op, d.ndim, d.kappa, d.npoints = 1, 3, 0.0, 2
+    d.nboxes, d.nlevels, d.root_level = 1, 1, 0
+    d.box_level, d.box_off, d.box_rank = (keep[k].ctypes.data for k in ("level", "off", "rank"))
+    d.entry_xyz, d.entry_pslot = keep["xyz"].ctypes.data, keep["pslot"].ctypes.data
+    d.nperm, d.perm_entry, d.perm_point = 2, keep["pe"].ctypes.data, keep["pp"].ctypes.data
+    d.t_off, d.t_data, d.t_len = keep["toff"].ctypes.data, keep["t"].ctypes.data, 1
+    d.list_off, d.list_src, d.list_kind = (keep[k].ctypes.data for k in ("loff", "lsrc", "lkind"))
+    h = ctypes.c_void_p()
+    assert lib.skf_plan_create(ctypes.byref(d), ctypes.byref(h)) == _lib.SKF_ERR_ARG
+    assert not h.value
+
+
+def test_python_api_rejects_non_finite_inputs():
+    """A NaN point, normal or charge is refused on the host with ValueError
+    (no build or device work starts)."""
+    import numpy as np
+
+    from skelfmm_gb300 import operators
+    from skelfmm_gb300.skel_fmm import SkelFMM
+
+    pts = np.random.default_rng(0).random((500, 3))
+    bad = pts.copy()
+    bad[7, 1] = np.nan
+    with pytest.raises(ValueError):
+        SkelFMM(bad, operators.LAPLACE_3D, tol=1e-6, leaf_size=64, defer_build=True)
+    geom = pts / np.linalg.norm(pts, axis=1, keepdims=True)
+    geom[3, 0] = np.inf
+    with pytest.raises(ValueError):
+        SkelFMM(pts, operators.LAPLACE_DOUBLE_LAYER_3D, geometry=geom, tol=1e-6, leaf_size=64, defer_build=True)
+    f = SkelFMM(pts, operators.LAPLACE_3D, tol=1e-6, leaf_size=64, defer_build=True)
+    f._is_built = True  # the charge check precedes any device work
+    q = np.ones(500)
+    q[11] = np.nan
+    with pytest.raises(ValueError):
+        f.apply(q)
+
+
+def test_max_bs_and_max_rank_must_be_integers():
+    """max_bs / max_rank are accepted (they pre-size the reference's padded
+    storage and never cap a rank); non-integers are refused."""
+    import numpy as np
+
+    from skelfmm_gb300 import operators
+    from skelfmm_gb300.skel_fmm import SkelFMM
+
+    pts = np.random.default_rng(0).random((500, 2))
+    with pytest.raises(ValueError):
+        SkelFMM(pts, operators.LAPLACE_2D, leaf_size=64, max_bs=10.5, max_rank=3, defer_build=True)
+    SkelFMM(pts, operators.LAPLACE_2D, leaf_size=64, max_bs=100, max_rank=3, defer_build=True)
