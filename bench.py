@@ -380,27 +380,49 @@ def ops_per_eval(opname, sym):
     return None
 
 
+KERNEL_NAMES = {
+    (1, 4): "k_translate_symw<{op}> (warps split the source tiles) + k_sym_reduce",
+    (1, 0): "k_translate_sym<{op}, 64, 5> + k_sym_reduce", (1, 1): "k_translate_sym<{op}, 128, 3> + k_sym_reduce",
+    (1, 2): "k_translate_sym<{op}, 64, 4> + k_sym_reduce", (1, 3): "k_translate_sym<{op}, 32, 5> + k_sym_reduce",
+}
+
+
 def roofline_line(plan, t_ms, opname, traffic_name):
+    """Roofline of the translation stage against the FP32 FMA pipe.
+
+    ``achieved``/``frac`` count the work as the reference's apply defines it:
+    every (target, source) pair of its lists, both directions and both the u
+    and the skeleton (uh) sums, at the per-pair FMA-pipe cost of one
+    evaluation (Laplace 3D: 3 differences, 3 for r^2, 1 multiply-add).  The
+    symmetric kernels evaluate a pair once for both directions, so the
+    figure credits that saving; ``frac_per_evaluation`` counts only the
+    evaluations the kernel performs (8 ops each for Laplace 3D: 3 + 3 + one
+    multiply-add per direction)."""
     peaks, src = measured_peaks()
     info = plan.info
     pairs = int(info.npairs_fused)
     evals = int(info.npairs_evaluated_mixed)
     sym = evals < pairs
-    ops = ops_per_eval(opname, sym)
+    ops_pair = ops_per_eval(opname, False)
+    ops_eval = ops_per_eval(opname, sym)
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    kern = (f"k_translate_sym<{opname.upper()}> + k_sym_reduce" if sym else
-            (f"k_translate_f32x2<{opname.upper()}>" if opname.startswith("laplace") else
-             ("k_translate_helm_x2 (packed FP32x2)" if opname == "helmholtz_3d" else
-              f"k_translate_f32<{opname.upper()}>")))
-    achieved = evals / (t_ms * 1e-3) / 1e9
-    peak = 152 * (128.0 / ops) * sm_mhz * 1e6 / 1e9
+    tuned = tuple(getattr(plan, "tuned", (1 if sym else 0, 0)))
+    opu = opname.upper()
+    kern = (KERNEL_NAMES.get(tuned, "k_translate_sym<{op}> + k_sym_reduce").format(op=opu) if sym else
+            (f"k_translate_f32x2<{opu}>" if opname.startswith("laplace") else
+             ("k_translate_helm_x2 (packed FP32x2)" if opname == "helmholtz_3d" else f"k_translate_f32<{opu}>")))
+    lane_ops = 152 * 128.0 * sm_mhz * 1e6  # FP32 FMA-pipe lane-ops per second
+    pairs_s = pairs / (t_ms * 1e-3)
+    evals_s = evals / (t_ms * 1e-3)
     return {
-        "bound": "fp32-fma", "kernel": kern, "achieved": round(achieved, 1), "peak": round(peak, 1),
-        "unit": "Geval/s", "frac": round(achieved / peak, 4), "traffic": profiled_traffic(traffic_name),
-        "peak_source": f"152 SMs x 128/{ops} evaluations/clk (FP32 FMA pipe, {ops} ops per evaluation) x "
-                       f"sm_max_mhz {sm_mhz:.0f} ({src} MEASURED_PEAKS.json clock); XU pipe not binding",
-        "evaluations_per_launch": evals, "pairs_per_launch": pairs, "launch_ms": round(t_ms, 4),
-        "pairs_per_s_G": round(pairs / (t_ms * 1e-3) / 1e9, 1),
+        "bound": "fp32-fma", "kernel": kern, "achieved": round(pairs_s / 1e9, 1),
+        "peak": round(lane_ops / ops_pair / 1e9, 1), "unit": "Gpair/s",
+        "frac": round(pairs_s * ops_pair / lane_ops, 4), "traffic": profiled_traffic(traffic_name),
+        "peak_source": f"152 SMs x 128 FP32 FMA-pipe lanes x sm_max_mhz {sm_mhz:.0f} ({src} MEASURED_PEAKS.json "
+                       f"clock) / {ops_pair} ops per target-source pair; XU pipe not binding",
+        "pairs_per_launch": pairs, "evaluations_per_launch": evals, "launch_ms": round(t_ms, 4),
+        "evaluations_per_s_G": round(evals_s / 1e9, 1),
+        "frac_per_evaluation": round(evals_s * ops_eval / lane_ops, 4),
     }
 
 

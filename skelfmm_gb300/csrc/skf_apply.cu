@@ -381,6 +381,17 @@ static void launch_sym(const SymArgs& c, int n, cudaStream_t st) {
   k_translate_sym<OP, TS, MINB><<<n, 128, smem, st>>>(c);
 }
 
+template <int OP>
+static void launch_symw(const SymArgs& c, int n, cudaStream_t st) {
+  constexpr size_t smem = symw_smem_bytes();
+  static bool attr = false;  // per instantiation
+  if (!attr) {
+    cudaFuncSetAttribute(k_translate_symw<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  k_translate_symw<OP><<<n, kSymwWarps * 32, smem, st>>>(c);
+}
+
 template <int TS, int MINB>
 static void launch_sym_helm(const SymArgs& c, float kappa, int n, cudaStream_t st) {
   constexpr size_t smem = symh_smem_bytes(TS);
@@ -452,6 +463,10 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
           c.pbuf = p->pbuf;
           c.u = p->u;
           c.uh = p->uh;
+          c.work_part = p->symw_part;
+          c.box_ntiles = p->box_ntiles;
+          c.box_nparts = p->box_nparts;
+          c.box_apart = p->box_apart;
           if constexpr (OP == SKF_HELMHOLTZ_3D) {
             if (p->worksym.n > 0) {
               // tile shape: 0 = 32 sources, 3 blocks/SM; 1 = 64 sources, 2 blocks/SM;
@@ -465,6 +480,14 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
             }
             k_sym_reduce_c<<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
                 p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
+          } else if (p->sym_shape == 4) {
+            // warps split the source tiles (k_translate_symw): its own items
+            // and incoming partial lists (A-side partials of split items)
+            c.work_box = p->worksymw.box;
+            c.work_row = p->worksymw.row;
+            if (p->worksymw.n > 0) launch_symw<OP>(c, p->worksymw.n, st);
+            k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
+                p->box_off, p->box_rank, p->in_off_w, p->in_blk_w, p->pbuf, p->u, p->uh);
           } else {
             if (p->worksym.n > 0) {
               // tile shape: 0 = 64 sources, 5 blocks/SM; 1 = 128 sources, 3 blocks/SM;

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -402,7 +403,82 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
       SKF_TRY(upload(p, &p->box_pstride, pstride.data(), pstride.size()));
       SKF_TRY(upload(p, &p->in_off, ioff.data(), ioff.size()));
       if (!iblk.empty()) SKF_TRY(upload(p, &p->in_blk, iblk.data(), iblk.size()));
+      // Source-split items for the warp-per-tile symmetric kernel (real
+      // operators): a box's owned tiles (32 sources, cut where the uh charges
+      // end, as the kernel cuts them) are numbered across its list; boxes
+      // whose items are far above an even share of the work get up to 8
+      // contiguous parts, so the launch has enough items to fill the GPU.
+      constexpr int kTileW = 32, kMaxParts = 8;
+      std::vector<int32_t> ntil(nb, 0), npart(nb, 1);
+      std::vector<int64_t> apart(nb, -1);
+      int64_t wcost_total = 0;
+      for (int A = 0; A < nb && !cplx; ++A) {
+        int64_t t = 0;
+        for (int64_t k = soff[A]; k < soff[A + 1]; ++k) {
+          const int B = ssrc[k];
+          const int kind = skind[k];
+          const int64_t bsB = d->box_off[B + 1] - d->box_off[B];
+          const int64_t nh = (kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_DOWN)
+                                 ? d->box_rank[B]
+                                 : (kind == SKF_KIND_COARSE_UP ? bsB : 0);
+          t += (nh + kTileW - 1) / kTileW + (bsB - nh + kTileW - 1) / kTileW;
+        }
+        ntil[A] = (int32_t)t;
+        wcost_total += (d->box_off[A + 1] - d->box_off[A]) * t;
+      }
+      // an even share for ~4 waves of 3 blocks per SM on 152 SMs
+      const double share = (double)wcost_total / (152.0 * 3.0 * 4.0);
+      int64_t aoff = total;
+      std::vector<std::vector<int64_t>> incoming_w = incoming;
+      std::vector<std::pair<int64_t, std::array<int32_t, 3>>> witems;
+      for (int A = 0; A < nb && !cplx; ++A) {
+        const int64_t bsA = d->box_off[A + 1] - d->box_off[A];
+        if (bsA == 0 || ntil[A] == 0) continue;
+        const double c = (double)std::min<int64_t>(tile, bsA) * ntil[A];
+        int P = (int)std::min<double>(kMaxParts, std::max(1.0, std::ceil(c / std::max(share, 1.0))));
+        P = std::min<int>(P, ntil[A]);
+        npart[A] = P;
+        if (P > 1) {
+          apart[A] = aoff;
+          for (int q = 1; q < P; ++q) {
+            // hi and lo halves of the part's row sums: two incoming blocks
+            incoming_w[A].push_back(aoff + (int64_t)(q - 1) * 4 * bsA);
+            incoming_w[A].push_back(aoff + (int64_t)(q - 1) * 4 * bsA + 2 * bsA);
+          }
+          aoff += (int64_t)(P - 1) * 4 * bsA;
+        }
+        for (int r0 = 0; r0 < bsA; r0 += tile)
+          for (int q = 0; q < P; ++q)
+            witems.push_back({std::min<int64_t>(tile, bsA - r0) * ((int64_t)(q + 1) * ntil[A] / P - (int64_t)q * ntil[A] / P),
+                              {A, r0, q}});
+      }
+      std::stable_sort(witems.begin(), witems.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+      std::vector<int32_t> wwb(witems.size()), wwr(witems.size()), wwq(witems.size());
+      for (size_t i = 0; i < witems.size(); ++i) {
+        wwb[i] = witems[i].second[0];
+        wwr[i] = witems[i].second[1];
+        wwq[i] = witems[i].second[2];
+      }
+      std::vector<int64_t> ioffw(nb + 1, 0), iblkw;
+      for (int B = 0; B < nb; ++B) {
+        ioffw[B + 1] = ioffw[B] + (int64_t)incoming_w[B].size();
+        iblkw.insert(iblkw.end(), incoming_w[B].begin(), incoming_w[B].end());
+      }
+      total = aoff;
+      SKF_TRY(upload(p, &p->box_ntiles, ntil.data(), ntil.size()));
+      SKF_TRY(upload(p, &p->box_nparts, npart.data(), npart.size()));
+      SKF_TRY(upload(p, &p->box_apart, apart.data(), apart.size()));
+      SKF_TRY(upload(p, &p->in_off_w, ioffw.data(), ioffw.size()));
+      if (!iblkw.empty()) SKF_TRY(upload(p, &p->in_blk_w, iblkw.data(), iblkw.size()));
+      p->worksymw.n = (int)witems.size();
+      if (p->worksymw.n > 0) {
+        SKF_TRY(upload(p, &p->worksymw.box, wwb.data(), wwb.size()));
+        SKF_TRY(upload(p, &p->worksymw.row, wwr.data(), wwr.size()));
+        SKF_TRY(upload(p, &p->symw_part, wwq.data(), wwq.size()));
+      }
       SKF_TRY(upload(p, &p->pbuf, (const float*)nullptr, (size_t)std::max<int64_t>(total, 1)));
+      // real operators default to the source-split kernel (shape 4)
+      if (!cplx) p->sym_shape = 4;
       p->worksym.n = (int)items.size();
       if (p->worksym.n > 0) {
         SKF_TRY(upload(p, &p->worksym.box, wb.data(), wb.size()));
@@ -491,7 +567,7 @@ int skf_plan_set_option(skf_plan* p, int32_t option, int64_t value) {
     case SKF_OPT_SCALAR_MIXED: p->scalar_mixed = value != 0; return SKF_OK;
     case SKF_OPT_SYMMETRIC: p->sym_on = value != 0; return SKF_OK;
     case SKF_OPT_SYM_SHAPE:
-      if (value < 0 || value > 3) return SKF_ERR_ARG;
+      if (value < 0 || value > 4) return SKF_ERR_ARG;
       p->sym_shape = (int)value;
       return SKF_OK;
     case SKF_OPT_PACKED_SHAPE:

@@ -66,6 +66,17 @@ struct skf_plan {
   int64_t* box_pstride = nullptr;
   int64_t* in_off = nullptr;
   int64_t* in_blk = nullptr;
+  // source-split symmetric kernel (SKF_OPT_SYM_SHAPE 4): items (box, row
+  // tile, part), a box's tiles split into box_nparts contiguous parts; parts
+  // past the first add their row sums through float-float A-side partial
+  // regions at box_apart (4 x bs floats per extra part), listed with the
+  // B-side partials in in_off_w / in_blk_w
+  int32_t* symw_part = nullptr;
+  int32_t* box_ntiles = nullptr;
+  int32_t* box_nparts = nullptr;
+  int64_t* box_apart = nullptr;
+  int64_t* in_off_w = nullptr;
+  int64_t* in_blk_w = nullptr;
   float* pbuf = nullptr;
   int64_t sym_pairs = 0;  // kernel evaluations per apply on the symmetric path
   int max_bs = 0;         // largest box
@@ -96,7 +107,7 @@ struct skf_plan {
   int64_t* list_off = nullptr;
   int32_t* list_src = nullptr;
   int8_t* list_kind = nullptr;
-  skf::WorkList work64, work32, worksym;
+  skf::WorkList work64, work32, worksym, worksymw;
   std::vector<skf::LevelBoxes> levels;  // indexed by level
   // apply vectors (scalars; complex: 2 doubles per entry)
   double* q = nullptr;

@@ -12,6 +12,8 @@
 // reproducible.  Coincident points only meet in U's self pair (identical
 // points share a box at every level), so only self pairs test r == 0.
 #pragma once
+#include <type_traits>
+
 #include "skf_internal.cuh"
 #include "skf_kernels.cuh"
 
@@ -810,6 +812,11 @@ struct SymArgs {
   float* pbuf;
   double* u;
   double* uh;
+  // source-split items (k_translate_symw only)
+  const int32_t* work_part;
+  const int32_t* box_ntiles;
+  const int32_t* box_nparts;
+  const int64_t* box_apart;
 };
 
 constexpr int kSymPairs = 2;  // packed row pairs per lane (4 rows)
@@ -1061,6 +1068,307 @@ __global__ void __launch_bounds__(128, MINB) k_translate_sym(SymArgs a) {
         a.u[offU + rb] = scale * v[1];
         a.uh[offU + rb] = rb < rU ? scale * v[3] : 0.0;
       }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ symmetric, warps split the sources
+// Same arithmetic and partial-buffer layout as k_translate_sym, organised so
+// that the source tiles need no thread-block barrier.  A block owns one part
+// of a 256-row work item: its share of the item's source tiles (32 sources,
+// numbered across the list entries; boxes with long lists split them into
+// box_nparts contiguous parts).  Each warp holds all 256 rows (8 per lane:
+// rows row0 + lane + 32 k, k < 8, packed in pairs (2p, 2p + 1)) and takes
+// every fourth tile of the part.  A warp stages its own tiles in a private,
+// double-buffered shared-memory area (the next tile is loaded into registers
+// while the current one is evaluated), so the B-side sums of a tile cover all
+// 256 rows inside one warp: lane l writes its sum for source j (over its 8
+// rows) to sT[j][l] (row stride 33: no bank conflicts either way) and, after
+// a warp barrier, lane j adds up row j and writes the tile's partial.  The
+// warps' row sums (compensated FP32 pairs) are added in FP64 in warp order
+// after one block barrier at the end; the first part writes u / uh, the
+// others float-float partials that k_sym_reduce adds: deterministic, no
+// atomics.
+constexpr int kSymwPairs = 4;   // packed row pairs per lane (8 rows)
+constexpr int kSymwWarps = 4;   // warps per block, splitting the part's source tiles
+__host__ __device__ constexpr int symw_ts() { return 32; }
+__host__ __device__ constexpr size_t symw_warp_bytes(int ts) {
+  return 2 * 4 * sizeof(ulonglong2) * (size_t)ts + 2 * sizeof(float) * (size_t)ts * 33;
+}
+__host__ __device__ constexpr size_t symw_smem_bytes() {
+  // per-warp tiles; the final row-sum exchange (warps x 256 rows x 4 floats) reuses them
+  return kSymwWarps * symw_warp_bytes(symw_ts()) > (size_t)kSymwWarps * 256 * 4 * sizeof(float)
+             ? kSymwWarps * symw_warp_bytes(symw_ts())
+             : (size_t)kSymwWarps * 256 * 4 * sizeof(float);
+}
+
+// NPA: packed row pairs that hold rows of the item (items shorter than 256
+// rows skip the pairs past their last row)
+template <int D, bool HR, bool HT, bool TR, bool SELF, bool LOG, int NPA>
+__device__ __forceinline__ void symw_tile(const ulonglong2* __restrict__ sb, int nt, int lane,
+                                          const f2_t (&thx)[kSymwPairs], const f2_t (&thy)[kSymwPairs],
+                                          const f2_t (&thz)[kSymwPairs], const f2_t (&tlx)[kSymwPairs],
+                                          const f2_t (&tly)[kSymwPairs], const f2_t (&tlz)[kSymwPairs],
+                                          const f2_t (&c1T)[kSymwPairs], const f2_t (&c2T)[kSymwPairs],
+                                          f2_t (&pu)[kSymwPairs], f2_t (&ph)[kSymwPairs], float* __restrict__ sTu,
+                                          float* __restrict__ sTh) {
+#pragma unroll 2
+  for (int j = 0; j < nt; ++j) {
+    const ulonglong2 A = sb[4 * j + 0];   // (-hx,-hx), (-hy,-hy)
+    const ulonglong2 B = sb[4 * j + 1];   // (-hz,-hz), (-lx,-lx)
+    const ulonglong2 Cc = sb[4 * j + 2];  // (-ly,-ly), (-lz,-lz)
+    const ulonglong2 Q = sb[4 * j + 3];   // (c1,c1), (c2,c2)
+    f2_t tu = 0ull, th = 0ull;
+#pragma unroll
+    for (int p = 0; p < NPA; ++p) {
+      const f2_t dx = f2_add(f2_add(thx[p], A.x), f2_add(tlx[p], B.y));
+      const f2_t dy = f2_add(f2_add(thy[p], A.y), f2_add(tly[p], Cc.x));
+      f2_t r2 = f2_mul(dx, dx);
+      r2 = f2_fma(dy, dy, r2);
+      if (D == 3) {
+        const f2_t dz = f2_add(f2_add(thz[p], B.x), f2_add(tlz[p], Cc.y));
+        r2 = f2_fma(dz, dz, r2);
+      }
+      float ra, rb;
+      f2_unpack(r2, ra, rb);
+      float ka = LOG ? lg2_approx(ra) : rsqrt_approx(ra);
+      float kb = LOG ? lg2_approx(rb) : rsqrt_approx(rb);
+      if (SELF) {
+        ka = ra > 0.f ? ka : 0.f;
+        kb = rb > 0.f ? kb : 0.f;
+      }
+      const f2_t k = f2_pack(ka, kb);
+      pu[p] = f2_fma(k, Q.x, pu[p]);
+      if (HR) ph[p] = f2_fma(k, Q.y, ph[p]);
+      if (TR) {
+        tu = p == 0 ? f2_mul(k, c1T[p]) : f2_fma(k, c1T[p], tu);
+        if (HT) th = p == 0 ? f2_mul(k, c2T[p]) : f2_fma(k, c2T[p], th);
+      }
+    }
+    if (TR) {
+      float a, b;
+      f2_unpack(tu, a, b);
+      sTu[j * 33 + lane] = a + b;
+      if (HT) {
+        f2_unpack(th, a, b);
+        sTh[j * 33 + lane] = a + b;
+      }
+    }
+  }
+}
+
+template <int OP>
+__global__ void __launch_bounds__(kSymwWarps * 32, 3) k_translate_symw(SymArgs a) {
+  constexpr int D = OpTraits<OP>::kDim;
+  constexpr bool LOG = (OP == SKF_LAPLACE_2D);
+  constexpr int TS = symw_ts();
+  constexpr int NP = kSymwPairs;
+  constexpr int NW = kSymwWarps;
+  extern __shared__ __align__(16) unsigned char symw_sm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* wsm = symw_sm + (size_t)warp * symw_warp_bytes(TS);
+  ulonglong2* sbuf = reinterpret_cast<ulonglong2*>(wsm);  // [2][TS][4]
+  float* sTu = reinterpret_cast<float*>(sbuf + 2 * 4 * TS);  // [TS][33]
+  float* sTh = sTu + TS * 33;
+
+  const int U = a.work_box[blockIdx.x];
+  const int row0 = a.work_row[blockIdx.x];
+  const int part = a.work_part[blockIdx.x];
+  const int64_t offU = a.box_off[U];
+  const int bsU = (int)(a.box_off[U + 1] - offU);
+  const int rU = a.box_rank[U];
+  const int64_t pbase = a.box_pbase[U] + (int64_t)(row0 / 256) * a.box_pstride[U];
+  // this part's tiles of the box's list: [g0, g1) in list order
+  const int ntot = a.box_ntiles[U], nparts = a.box_nparts[U];
+  const int g0 = (int)((int64_t)part * ntot / nparts), g1 = (int)((int64_t)(part + 1) * ntot / nparts);
+
+  f2_t thx[NP], thy[NP], thz[NP], tlx[NP], tly[NP], tlz[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const int ra = row0 + lane + 64 * p, rb = ra + 32;
+    const int64_t ea = offU + min(ra, bsU - 1), eb = offU + min(rb, bsU - 1);
+    const float4 ha = a.hi32[ea], hb = a.hi32[eb];
+    const float4 la = a.lo32[ea], lb = a.lo32[eb];
+    thx[p] = f2_pack(ha.x, hb.x);
+    thy[p] = f2_pack(ha.y, hb.y);
+    thz[p] = f2_pack(ha.z, hb.z);
+    tlx[p] = f2_pack(la.x, lb.x);
+    tly[p] = f2_pack(la.y, lb.y);
+    tlz[p] = f2_pack(la.z, lb.z);
+  }
+  const bool skel_rows = row0 < rU;
+  // packed pairs holding rows of this item: pair p holds rows 64 p .. 64 p + 63
+  const int nrows = min(256, bsU - row0);
+  const int npa = nrows <= 64 ? 1 : (nrows <= 128 ? 2 : 4);
+  const f2_t zero = 0ull;
+  f2_t su[NP], cu[NP], sh[NP], ch[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) su[p] = cu[p] = sh[p] = ch[p] = zero;
+
+  int gbase = 0;  // tiles of the earlier list entries (the warp of tile g is g % NW)
+  const int64_t l0 = a.list_off[U], l1 = a.list_off[U + 1];
+  for (int64_t l = l0; l < l1 && gbase < g1; ++l) {
+    const int s = a.list_src[l];
+    const int64_t offS = a.box_off[s];
+    const int bsS = (int)(a.box_off[s + 1] - offS);
+    if (bsS == 0) continue;
+    const int kind = a.list_kind[l];
+    const int rS = a.box_rank[s];
+    const bool self = (s == U);
+    const int nh = (kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_DOWN)
+                       ? rS
+                       : ((kind == SKF_KIND_COARSE_UP) ? bsS : 0);
+    // tiles: [0, nh) and [nh, bsS) in chunks of TS (sources past nh carry no
+    // uh charge); the plan counts them the same way (box_ntiles)
+    const int nth = (nh + TS - 1) / TS;
+    const int ntiles = nth + (bsS - nh + TS - 1) / TS;
+    // this warp's tiles of the entry: local k with gbase + k in [g0, g1), = warp (mod NW)
+    const int kmin = max(0, g0 - gbase), kend = min(ntiles, g1 - gbase);
+    int k = kmin + ((warp - (gbase + kmin)) % NW + NW) % NW;
+    gbase += ntiles;
+    if (k >= kend) continue;
+    auto tile_t0 = [&](int kk) { return kk < nth ? kk * TS : nh + (kk - nth) * TS; };
+    auto tile_len = [&](int kk) { return kk < nth ? min(TS, nh - kk * TS) : min(TS, bsS - tile_t0(kk)); };
+    const float* c1src = (kind == SKF_KIND_COARSE_DOWN) ? a.qd32 : a.q32;
+    // charges of this item's rows seen from the source box (mirror kind)
+    f2_t c1T[NP], c2T[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) c1T[p] = c2T[p] = zero;
+    if (!self) {
+      const float* t1 = (kind == SKF_KIND_COARSE_UP) ? a.qd32 : a.q32;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const int ra = row0 + lane + 64 * p, rb = ra + 32;
+        const float ca = ra < bsU ? t1[offU + ra] : 0.f, cb = rb < bsU ? t1[offU + rb] : 0.f;
+        c1T[p] = f2_pack(ca, cb);
+        float da = 0.f, db = 0.f;
+        if (kind == SKF_KIND_COLLEAGUE) {
+          da = ra < bsU ? a.qhn32[offU + ra] : 0.f;
+          db = rb < bsU ? a.qhn32[offU + rb] : 0.f;
+        } else if (kind == SKF_KIND_COARSE_DOWN) {
+          da = -ca;
+          db = -cb;
+        }
+        c2T[p] = f2_pack(da, db);
+      }
+    }
+    const bool row_h_kind = kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_UP;
+    const bool t_h_kind = kind == SKF_KIND_COLLEAGUE ? skel_rows : kind == SKF_KIND_COARSE_DOWN;
+    const bool hr_kind = row_h_kind && skel_rows;
+    const int64_t pblk = self ? 0 : pbase + a.list_poff[l];
+    // source j of tile kk, as loaded by lane j
+    float4 nh4 = make_float4(0, 0, 0, 0), nl4 = nh4;
+    float nc1 = 0.f, nc2 = 0.f;
+    auto load_src = [&](int kk) {
+      if (lane < tile_len(kk)) {
+        const int64_t e = offS + tile_t0(kk) + lane;
+        nh4 = a.hi32[e];
+        nl4 = a.lo32[e];
+        nc1 = c1src[e];
+        nc2 = kind == SKF_KIND_COLLEAGUE ? a.qhn32[e] : (kind == SKF_KIND_COARSE_UP ? -nc1 : 0.f);
+      }
+    };
+    auto store_src = [&](ulonglong2* dst) {
+      dst[4 * lane + 0] = make_ulonglong2(f2_pack(-nh4.x, -nh4.x), f2_pack(-nh4.y, -nh4.y));
+      dst[4 * lane + 1] = make_ulonglong2(f2_pack(-nh4.z, -nh4.z), f2_pack(-nl4.x, -nl4.x));
+      dst[4 * lane + 2] = make_ulonglong2(f2_pack(-nl4.y, -nl4.y), f2_pack(-nl4.z, -nl4.z));
+      dst[4 * lane + 3] = make_ulonglong2(f2_pack(nc1, nc1), f2_pack(nc2, nc2));
+    };
+    int buf = 0;
+    load_src(k);
+    __syncwarp();
+    store_src(sbuf);
+    for (; k < kend; k += NW) {
+      const int t0 = tile_t0(k);
+      const int nt = tile_len(k);
+      const bool hseg = k < nth;
+      const bool more = k + NW < kend;
+      if (more) load_src(k + NW);  // this warp's next tile, in flight during this one
+      __syncwarp();
+      const ulonglong2* sb = sbuf + buf * 4 * TS;
+      const bool hr = hseg && hr_kind;
+      const bool ht = hseg && t_h_kind;
+      f2_t pu[NP], ph[NP];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) pu[p] = ph[p] = zero;
+      auto run = [&](auto npa_tag) {
+        constexpr int NPA = decltype(npa_tag)::value;
+        if (self) {
+          if (hr) symw_tile<D, true, false, false, true, LOG, NPA>(sb, nt, lane, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, sTu, sTh);
+          else symw_tile<D, false, false, false, true, LOG, NPA>(sb, nt, lane, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, sTu, sTh);
+        } else if (hr) {
+          if (ht) symw_tile<D, true, true, true, false, LOG, NPA>(sb, nt, lane, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, sTu, sTh);
+          else symw_tile<D, true, false, true, false, LOG, NPA>(sb, nt, lane, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, sTu, sTh);
+        } else {
+          if (ht) symw_tile<D, false, true, true, false, LOG, NPA>(sb, nt, lane, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, sTu, sTh);
+          else symw_tile<D, false, false, true, false, LOG, NPA>(sb, nt, lane, thx, thy, thz, tlx, tly, tlz, c1T, c2T, pu, ph, sTu, sTh);
+        }
+      };
+      if (npa == 4) run(std::integral_constant<int, 4>());
+      else if (npa == 2) run(std::integral_constant<int, 2>());
+      else run(std::integral_constant<int, 1>());
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        f2_two_sum(su[p], cu[p], pu[p]);
+        if (hr) f2_two_sum(sh[p], ch[p], ph[p]);
+      }
+      __syncwarp();
+      if (!self && lane < nt) {
+        // lane j: the tile's B-side sums of source j over the item's 256 rows
+        float vu = 0.f, vh = 0.f;
+#pragma unroll 8
+        for (int r = 0; r < 32; ++r) vu += sTu[lane * 33 + r];
+        if (ht) {
+#pragma unroll 8
+          for (int r = 0; r < 32; ++r) vh += sTh[lane * 33 + r];
+        }
+        a.pbuf[pblk + t0 + lane] = vu;
+        a.pbuf[pblk + bsS + t0 + lane] = vh;
+      }
+      if (more) store_src(sbuf + (buf ^ 1) * 4 * TS);
+      __syncwarp();
+      buf ^= 1;
+    }
+  }
+  // row sums of the warps, added in FP64 in warp order
+  __syncthreads();
+  float* ex = reinterpret_cast<float*>(symw_sm);  // [NW][256][4]: su, cu, sh, ch
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    float v[8];
+    f2_unpack(su[p], v[0], v[4]);
+    f2_unpack(cu[p], v[1], v[5]);
+    f2_unpack(sh[p], v[2], v[6]);
+    f2_unpack(ch[p], v[3], v[7]);
+    const int ra = lane + 64 * p, rb = ra + 32;
+    *reinterpret_cast<float4*>(ex + ((size_t)warp * 256 + ra) * 4) = make_float4(v[0], v[1], v[2], v[3]);
+    *reinterpret_cast<float4*>(ex + ((size_t)warp * 256 + rb) * 4) = make_float4(v[4], v[5], v[6], v[7]);
+  }
+  __syncthreads();
+  const double scale = LOG ? 0.34657359027997264 : 1.0;
+  // the first part owns u / uh; later parts leave float-float partials
+  // (hi region, then lo region) that k_sym_reduce adds in a fixed order
+  float* apart = part > 0 ? a.pbuf + a.box_apart[U] + (int64_t)(part - 1) * 4 * bsU : nullptr;
+  for (int r = threadIdx.x; r < 256; r += NW * 32) {
+    const int row = row0 + r;
+    if (row >= bsU) continue;
+    double vu = 0.0, vh = 0.0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      const float4 e = *reinterpret_cast<const float4*>(ex + ((size_t)w * 256 + r) * 4);
+      vu += (double)e.x + (double)e.y;
+      vh += (double)e.z + (double)e.w;
+    }
+    if (row >= rU) vh = 0.0;
+    if (part == 0) {
+      a.u[offU + row] = scale * vu;
+      a.uh[offU + row] = scale * vh;
+    } else {
+      const float hu = (float)vu, hh = (float)vh;
+      apart[row] = hu;
+      apart[bsU + row] = hh;
+      apart[2 * bsU + row] = (float)(vu - (double)hu);
+      apart[3 * bsU + row] = (float)(vh - (double)hh);
     }
   }
 }

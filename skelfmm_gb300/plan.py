@@ -249,7 +249,8 @@ class Plan:
         self.set_option(_lib.OPT_SYMMETRIC, 1)
         info = self._query()
         sym_ok = info.npairs_evaluated_mixed < info.npairs_fused
-        cands = ([(1, sh) for sh in range(4)] if sym_ok else []) + [(0, sh) for sh in range(3)]
+        nsym = 4 if self.is_complex else 5  # shape 4: the source-split Laplace kernel
+        cands = ([(1, sh) for sh in range(nsym)] if sym_ok else []) + [(0, sh) for sh in range(3)]
         results = {}
         for sym, shape in cands:
             self.set_option(_lib.OPT_SYMMETRIC, sym)

@@ -114,20 +114,24 @@ def test_symmetric_translations_agree(name):
     assert np.array_equal(y2, y_sym)  # deterministic
 
 
-@pytest.mark.parametrize("name", ["lap3d_cube", "helm3d_sphere"])
+@pytest.mark.parametrize("name", ["lap3d_cube", "lap3d_c2params", "lap2d_annulus", "helm3d_sphere"])
 def test_symmetric_tile_shapes_agree(name):
     """Every tile shape of the symmetric kernel (sources per tile, blocks per
-    SM) gives the same apply up to the order of the partial sums."""
+    SM, and the source-split kernel) gives the same apply up to the order of
+    the partial sums; each is deterministic."""
     from skelfmm_gb300 import _lib
 
     d, plan = _plan(name)
     x = np.ascontiguousarray(d["x"])
     ys = []
-    for shape in range(4):
+    for shape in range(5):
         plan.set_option(_lib.OPT_SYM_SHAPE, shape)
         y = np.empty_like(x)
         plan.apply_host(x, y, _lib.PREC_MIXED)
         ys.append(y)
+        y2 = np.empty_like(x)
+        plan.apply_host(x, y2, _lib.PREC_MIXED)
+        assert np.array_equal(y2, y)
     plan.set_option(_lib.OPT_SYM_SHAPE, 0)
     for y in ys[1:]:
         assert relinf(y, ys[0]) < 1e-6
