@@ -477,6 +477,16 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
         SKF_TRY(upload(p, &p->symw_part, wwq.data(), wwq.size()));
       }
       SKF_TRY(upload(p, &p->pbuf, (const float*)nullptr, (size_t)std::max<int64_t>(total, 1)));
+      {
+        // partial slots a kernel never writes (uh partials of tiles without uh
+        // charges, skipped by k_translate_symw) must read as zero
+        const cudaError_t e = cudaMemset(p->pbuf, 0, sizeof(float) * (size_t)std::max<int64_t>(total, 1));
+        if (e != cudaSuccess) {
+          set_last_cuda_error(e);
+          free_plan(p);
+          return SKF_ERR_CUDA;
+        }
+      }
       // real operators default to the source-split kernel (shape 4)
       if (!cplx) p->sym_shape = 4;
       p->worksym.n = (int)items.size();

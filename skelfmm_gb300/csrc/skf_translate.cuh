@@ -1084,7 +1084,8 @@ __global__ void __launch_bounds__(128, MINB) k_translate_sym(SymArgs a) {
 // while the current one is evaluated), so the B-side sums of a tile cover all
 // 256 rows inside one warp: lane l writes its sum for source j (over its 8
 // rows) to sT[j][l] (row stride 33: no bank conflicts either way) and, after
-// a warp barrier, lane j adds up row j and writes the tile's partial.  The
+// a warp barrier, lane j adds up row j and writes the tile's partial (uh
+// partials only where the tile carries uh sums; the others stay zero).  The
 // warps' row sums (compensated FP32 pairs) are added in FP64 in warp order
 // after one block barrier at the end; the first part writes u / uh, the
 // others float-float partials that k_sym_reduce adds: deterministic, no
@@ -1114,10 +1115,10 @@ __device__ __forceinline__ void symw_tile(const ulonglong2* __restrict__ sb, int
                                           float* __restrict__ sTh) {
 #pragma unroll 2
   for (int j = 0; j < nt; ++j) {
-    const ulonglong2 A = sb[4 * j + 0];   // (-hx,-hx), (-hy,-hy)
-    const ulonglong2 B = sb[4 * j + 1];   // (-hz,-hz), (-lx,-lx)
-    const ulonglong2 Cc = sb[4 * j + 2];  // (-ly,-ly), (-lz,-lz)
-    const ulonglong2 Q = sb[4 * j + 3];   // (c1,c1), (c2,c2)
+    const ulonglong2 A = sb[j];                     // (-hx,-hx), (-hy,-hy)
+    const ulonglong2 B = sb[symw_ts() + j];         // (-hz,-hz), (-lx,-lx)
+    const ulonglong2 Cc = sb[2 * symw_ts() + j];    // (-ly,-ly), (-lz,-lz)
+    const ulonglong2 Q = sb[3 * symw_ts() + j];     // (c1,c1), (c2,c2)
     f2_t tu = 0ull, th = 0ull;
 #pragma unroll
     for (int p = 0; p < NPA; ++p) {
@@ -1268,11 +1269,11 @@ __global__ void __launch_bounds__(kSymwWarps * 32, 3) k_translate_symw(SymArgs a
         nc2 = kind == SKF_KIND_COLLEAGUE ? a.qhn32[e] : (kind == SKF_KIND_COARSE_UP ? -nc1 : 0.f);
       }
     };
-    auto store_src = [&](ulonglong2* dst) {
-      dst[4 * lane + 0] = make_ulonglong2(f2_pack(-nh4.x, -nh4.x), f2_pack(-nh4.y, -nh4.y));
-      dst[4 * lane + 1] = make_ulonglong2(f2_pack(-nh4.z, -nh4.z), f2_pack(-nl4.x, -nl4.x));
-      dst[4 * lane + 2] = make_ulonglong2(f2_pack(-nl4.y, -nl4.y), f2_pack(-nl4.z, -nl4.z));
-      dst[4 * lane + 3] = make_ulonglong2(f2_pack(nc1, nc1), f2_pack(nc2, nc2));
+    auto store_src = [&](ulonglong2* dst) {  // planes [4][TS]
+      dst[lane] = make_ulonglong2(f2_pack(-nh4.x, -nh4.x), f2_pack(-nh4.y, -nh4.y));
+      dst[TS + lane] = make_ulonglong2(f2_pack(-nh4.z, -nh4.z), f2_pack(-nl4.x, -nl4.x));
+      dst[2 * TS + lane] = make_ulonglong2(f2_pack(-nl4.y, -nl4.y), f2_pack(-nl4.z, -nl4.z));
+      dst[3 * TS + lane] = make_ulonglong2(f2_pack(nc1, nc1), f2_pack(nc2, nc2));
     };
     int buf = 0;
     load_src(k);
@@ -1323,7 +1324,9 @@ __global__ void __launch_bounds__(kSymwWarps * 32, 3) k_translate_symw(SymArgs a
           for (int r = 0; r < 32; ++r) vh += sTh[lane * 33 + r];
         }
         a.pbuf[pblk + t0 + lane] = vu;
-        a.pbuf[pblk + bsS + t0 + lane] = vh;
+        // uh partials of tiles without uh charges stay at the zeros the
+        // plan wrote when it allocated the buffer (the same slots every apply)
+        if (ht) a.pbuf[pblk + bsS + t0 + lane] = vh;
       }
       if (more) store_src(sbuf + (buf ^ 1) * 4 * TS);
       __syncwarp();

@@ -148,6 +148,65 @@ def ragged_from_reference(tree, fmm, operator, kappa=0.0):
     )
 
 
+# ------------------------------------------------------------------ saved builds
+# A built operator on disk: the ragged description (the arrays skf_plan_create
+# takes) in one numpy .npz archive, with a format tag, a version and the
+# scalar type of T.  Loading it and creating a plan gives the same apply, bit
+# for bit, as the plan it was saved from; a build made anywhere (the GPU
+# build, a CPU build in the reference's layout through ragged_from_reference)
+# can be saved and replayed on the GPU later.
+FORMAT_TAG = "skelfmm_gb300.ragged_build"
+FORMAT_VERSION = 1
+_ARRAYS = ("box_level", "box_off", "box_rank", "entry_xyz", "entry_pslot", "perm_entry", "perm_point", "t_off",
+           "t_data", "list_off", "list_src", "list_kind")
+_DTYPES = {"box_level": np.int32, "box_off": np.int64, "box_rank": np.int32, "entry_xyz": np.float64,
+           "entry_pslot": np.int64, "perm_entry": np.int64, "perm_point": np.int64, "t_off": np.int64,
+           "list_off": np.int64, "list_src": np.int32, "list_kind": np.int8}
+
+
+def save_ragged(rb: RaggedBuild, path, extra=None):
+    """Write ``rb`` (T copied to the host if it is on the device) to ``path``
+    (.npz).  ``extra``: further named arrays stored beside it."""
+    t = rb.t_data.detach().cpu().numpy() if isinstance(rb.t_data, torch.Tensor) else np.asarray(rb.t_data)
+    out = {"format": np.array(FORMAT_TAG), "version": np.array(FORMAT_VERSION),
+           "t_dtype": np.array(str(t.dtype)),
+           "scalars": np.array([rb.op, rb.ndim, rb.npoints, rb.nlevels, rb.root_level], dtype=np.int64),
+           "kappa": np.array(rb.kappa, dtype=np.float64)}
+    for k in _ARRAYS:
+        out[k] = t if k == "t_data" else np.ascontiguousarray(getattr(rb, k), dtype=_DTYPES[k])
+    if rb.entry_geom is not None:
+        out["entry_geom"] = np.ascontiguousarray(rb.entry_geom, dtype=np.float64)
+    for k, v in (extra or {}).items():
+        out["extra/" + k] = np.asarray(v)
+    with open(path, "wb") as f:
+        np.savez(f, **out)
+
+
+def load_ragged(path):
+    """(RaggedBuild, extra) from a file written by save_ragged; ValueError
+    for another format, a newer version or inconsistent arrays."""
+    with np.load(path, allow_pickle=False) as d:
+        if "format" not in d.files or str(d["format"]) != FORMAT_TAG:
+            raise ValueError(f"{path}: not a saved skelfmm_gb300 build")
+        if int(d["version"]) > FORMAT_VERSION:
+            raise ValueError(f"{path}: format version {int(d['version'])} is newer than {FORMAT_VERSION}")
+        op, ndim, npoints, nlevels, root_level = (int(v) for v in d["scalars"])
+        arrs = {k: d[k] for k in _ARRAYS}
+        if str(arrs["t_data"].dtype) != str(d["t_dtype"]) or \
+                arrs["t_data"].dtype != (np.complex128 if is_complex_op(op) else np.float64):
+            raise ValueError(f"{path}: T blocks have the wrong scalar type for the operator")
+        geom = d["entry_geom"] if "entry_geom" in d.files else None
+        extra = {k[6:]: d[k] for k in d.files if k.startswith("extra/")}
+        kappa = float(d["kappa"])
+    nb = arrs["box_level"].shape[0]
+    if arrs["box_off"].shape[0] != nb + 1 or arrs["list_off"].shape[0] != nb + 1 or \
+            arrs["entry_xyz"].shape[0] != int(arrs["box_off"][-1]):
+        raise ValueError(f"{path}: inconsistent array sizes")
+    rb = RaggedBuild(op=op, ndim=ndim, kappa=kappa, npoints=npoints, nlevels=nlevels, root_level=root_level,
+                     entry_geom=geom, **arrs)
+    return rb, extra
+
+
 # translation kernel variants (operator, precision, symmetric, shape) that
 # have run in this process: their first launch carries the module load
 _WARMED = set()
@@ -213,6 +272,16 @@ class Plan:
     @property
     def handle(self):
         return self._h
+
+    def save(self, path):
+        """Write the plan's build to ``path`` (see save_ragged)."""
+        save_ragged(self.rb, path)
+
+    @classmethod
+    def load(cls, path):
+        """A plan on the current device from a file written by ``save``."""
+        rb, _ = load_ragged(path)
+        return cls(rb)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

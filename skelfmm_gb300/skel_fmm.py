@@ -22,7 +22,7 @@ import torch
 
 from . import _lib
 from .operators import _require_operator, cuda_op_id, is_complex_op
-from .plan import Plan
+from .plan import Plan, load_ragged, save_ragged
 from .recursive_skel import RecursiveSkeletonization
 from .tree import BalancedTree
 
@@ -85,7 +85,8 @@ class SkelFMM:
 
     def __init__(self, points, operator, geometry=None, tol=1e-5, rank_or_tol=None, leaf_size=200,
                  use_single_precision=False, param=0.0, quiet=True, keep_host_fmm=False, defer_build=False,
-                 npoints_max=500, p="auto", max_bs=-1, max_rank=-1, precision=None, learned_rank=False):
+                 npoints_max=500, p="auto", max_bs=-1, max_rank=-1, precision=None, learned_rank=False,
+                 cuda_graph=False):
         self.points = np.asarray(points, dtype=np.float64)
         if self.points.ndim != 2 or not np.all(np.isfinite(self.points)):
             raise ValueError("points must be a finite [N, ndim] array")
@@ -126,6 +127,11 @@ class SkelFMM:
         self.fmm = None
         self.plan = None
         self.batched = None
+        # cuda_graph: record one apply of the built operator into a CUDA graph
+        # (capture()); applies then replay it on static device buffers
+        self._cuda_graph = bool(cuda_graph)
+        self._graph = None
+        self._gx = self._gy = None
         self.device = torch.device("cuda") if torch.cuda.is_available() else None
         self.kernel_backend = "cuda-sm103a"
         self.tree_time_seconds = 0.0
@@ -199,7 +205,72 @@ class SkelFMM:
         self.total_storage_bytes = self.host_storage_bytes + self.device_storage_bytes
         self.nbytes = self.total_storage_bytes
         self._is_built = True
+        if self._cuda_graph:
+            self.capture()
         return self
+
+    def capture(self):
+        """Record one device apply of the built operator into a CUDA graph.
+
+        The graph works on two device vectors owned by this object; ``apply``
+        and ``apply_device`` then copy the charges in, replay the graph (one
+        launch of the whole apply: permutation, upward passes, translations,
+        partial sums, downward passes) and copy the potentials out.  The
+        replay performs the same kernels on the same data as the eager apply,
+        so its results are bitwise equal."""
+        self._ensure_built()
+        dt = torch.complex128 if is_complex_op(self.operator) else torch.float64
+        n = self.points.shape[0]
+        self._gx = torch.zeros(n, dtype=dt, device=self.device)
+        self._gy = torch.zeros(n, dtype=dt, device=self.device)
+        # first launches (kernel attributes, module loading) outside the capture
+        self.plan.apply_device(self._gx, self._gy, self._prec_code, torch.cuda.current_stream(self.device).cuda_stream)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=torch.cuda.Stream(self.device)):
+            self.plan.apply_device(self._gx, self._gy, self._prec_code, torch.cuda.current_stream().cuda_stream)
+        self._graph = g
+        return g
+
+    def save(self, path):
+        """Write the built operator to ``path`` (.npz): its ragged build and
+        the points, operator, parameter, tolerance and leaf size, so that
+        ``SkelFMM.load`` can apply it without building again."""
+        self._ensure_built()
+        extra = {"points": self.points, "operator": np.array(self.operator.name),
+                 "param": np.array(float(self.param)), "tol": np.array(float(self.rank_or_tol)),
+                 "leaf_size": np.array(int(self.leaf_size)), "precision": np.array(self.precision)}
+        if self.geometry is not None:
+            extra["geometry"] = np.asarray(self.geometry, dtype=np.float64)
+        save_ragged(self.plan.rb, path, extra)
+
+    @classmethod
+    def load(cls, path, *, precision=None, cuda_graph=False):
+        """A built operator from a file written by ``save`` (or by
+        ``plan.save_ragged`` with the same extra fields), on the current
+        device; ``precision`` overrides the saved one."""
+        from .operators import BY_NAME
+
+        rb, extra = load_ragged(path)
+        op = BY_NAME[str(extra["operator"])]
+        geom = extra.get("geometry")
+        obj = cls(extra["points"], op, geometry=geom, tol=float(extra["tol"]), leaf_size=int(extra["leaf_size"]),
+                  param=float(extra["param"]), precision=precision or str(extra["precision"]), defer_build=True,
+                  cuda_graph=cuda_graph)
+        if cuda_op_id(op) != rb.op or rb.npoints != obj.points.shape[0]:
+            raise ValueError(f"{path}: build and stored operator or points disagree")
+        t0 = perf_counter()
+        obj.plan = Plan(rb)
+        obj.tuning = obj.plan.autotune(obj._prec_code, reps=2) if obj._prec_code != _lib.PREC_FP64 else None
+        obj.nlevels, obj.nboxes = rb.nlevels, rb.nboxes
+        obj.rank_max = int(np.max(rb.box_rank)) if rb.nboxes else 0
+        obj.device_storage_bytes = int(obj.plan.info.device_bytes)
+        obj.total_storage_bytes = obj.nbytes = obj.device_storage_bytes
+        obj.setup_time_seconds = obj.build_time_seconds = perf_counter() - t0
+        obj._is_built = True
+        if cuda_graph:
+            obj.capture()
+        return obj
 
     def _ensure_built(self, *, announce=False):
         if getattr(self, "_is_built", True):
@@ -226,8 +297,13 @@ class SkelFMM:
             return re + 1j * im
         dt = np.complex128 if cplx else np.float64
         xin = np.ascontiguousarray(x_np, dtype=dt)
-        y = np.empty_like(xin)
-        self.plan.apply_host(xin, y, self._prec_code)
+        if self._graph is not None:
+            self._gx.copy_(torch.from_numpy(xin))
+            self._graph.replay()
+            y = self._gy.cpu().numpy()
+        else:
+            y = np.empty_like(xin)
+            self.plan.apply_host(xin, y, self._prec_code)
         if not cplx and self._use_single_precision:
             return y.astype(np.float32)
         if cplx and self._use_single_precision:
@@ -245,6 +321,11 @@ class SkelFMM:
         x = x.to(dtype=dt).contiguous()
         if y is None:
             y = torch.empty_like(x)
+        if self._graph is not None:
+            self._gx.copy_(x)
+            self._graph.replay()
+            y.copy_(self._gy)
+            return y
         self.plan.apply_device(x, y, self._prec_code, torch.cuda.current_stream(x.device).cuda_stream)
         return y
 
