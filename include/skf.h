@@ -132,7 +132,8 @@ int skf_plan_apply_host(skf_plan* plan, const void* x_host, void* y_host, int32_
    shared-memory tile and 5 blocks per SM (default for Helmholtz 3D), 1 = 128
    and 3, 2 = 64 and 4, 3 = 32 and 5; 4 = warps splitting the source tiles of
    256-row items without block barriers (default for Laplace 2D/3D; Helmholtz
-   3D plans treat it as 0). */
+   3D plans treat it as 0); 5 = as 4 with persistent blocks taking the items
+   from a queue. */
 #define SKF_OPT_SYM_SHAPE 4
 int skf_plan_set_option(skf_plan* plan, int32_t option, int64_t value);
 

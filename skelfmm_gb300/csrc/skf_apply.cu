@@ -382,14 +382,23 @@ static void launch_sym(const SymArgs& c, int n, cudaStream_t st) {
 }
 
 template <int OP>
-static void launch_symw(const SymArgs& c, int n, cudaStream_t st) {
+static void launch_symw(const SymArgs& c, int n, int* queue, cudaStream_t st) {
   constexpr size_t smem = symw_smem_bytes();
   static bool attr = false;  // per instantiation
   if (!attr) {
     cudaFuncSetAttribute(k_translate_symw<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_translate_symw_queue<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  k_translate_symw<OP><<<n, kSymwWarps * 32, smem, st>>>(c);
+  if (queue == nullptr) {
+    k_translate_symw<OP><<<n, kSymwWarps * 32, smem, st>>>(c);
+  } else {
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaMemsetAsync(queue, 0, sizeof(int), st);
+    k_translate_symw_queue<OP><<<std::min(n, 3 * nsm), kSymwWarps * 32, smem, st>>>(c, n, queue);
+  }
 }
 
 template <int TS, int MINB>
@@ -480,12 +489,13 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
             }
             k_sym_reduce_c<<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
                 p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
-          } else if (p->sym_shape == 4) {
+          } else if (p->sym_shape == 4 || p->sym_shape == 5) {
             // warps split the source tiles (k_translate_symw): its own items
-            // and incoming partial lists (A-side partials of split items)
+            // and incoming partial lists (A-side partials of split items);
+            // shape 5 takes the items from a queue with persistent blocks
             c.work_box = p->worksymw.box;
             c.work_row = p->worksymw.row;
-            if (p->worksymw.n > 0) launch_symw<OP>(c, p->worksymw.n, st);
+            if (p->worksymw.n > 0) launch_symw<OP>(c, p->worksymw.n, p->sym_shape == 5 ? p->symw_queue : nullptr, st);
             k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
                 p->box_off, p->box_rank, p->in_off_w, p->in_blk_w, p->pbuf, p->u, p->uh);
           } else {

@@ -470,6 +470,7 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
       SKF_TRY(upload(p, &p->box_apart, apart.data(), apart.size()));
       SKF_TRY(upload(p, &p->in_off_w, ioffw.data(), ioffw.size()));
       if (!iblkw.empty()) SKF_TRY(upload(p, &p->in_blk_w, iblkw.data(), iblkw.size()));
+      SKF_TRY(upload(p, &p->symw_queue, (const int*)nullptr, 1));
       p->worksymw.n = (int)witems.size();
       if (p->worksymw.n > 0) {
         SKF_TRY(upload(p, &p->worksymw.box, wwb.data(), wwb.size()));
@@ -577,7 +578,7 @@ int skf_plan_set_option(skf_plan* p, int32_t option, int64_t value) {
     case SKF_OPT_SCALAR_MIXED: p->scalar_mixed = value != 0; return SKF_OK;
     case SKF_OPT_SYMMETRIC: p->sym_on = value != 0; return SKF_OK;
     case SKF_OPT_SYM_SHAPE:
-      if (value < 0 || value > 4) return SKF_ERR_ARG;
+      if (value < 0 || value > 5) return SKF_ERR_ARG;
       p->sym_shape = (int)value;
       return SKF_OK;
     case SKF_OPT_PACKED_SHAPE:

@@ -77,6 +77,7 @@ struct skf_plan {
   int64_t* box_apart = nullptr;
   int64_t* in_off_w = nullptr;
   int64_t* in_blk_w = nullptr;
+  int* symw_queue = nullptr;  // item counter of the persistent form (shape 5)
   float* pbuf = nullptr;
   int64_t sym_pairs = 0;  // kernel evaluations per apply on the symmetric path
   int max_bs = 0;         // largest box

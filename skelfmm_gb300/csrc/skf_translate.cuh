@@ -1159,7 +1159,7 @@ __device__ __forceinline__ void symw_tile(const ulonglong2* __restrict__ sb, int
 }
 
 template <int OP>
-__global__ void __launch_bounds__(kSymwWarps * 32, 3) k_translate_symw(SymArgs a) {
+__device__ __forceinline__ void symw_item(const SymArgs& a, int item) {
   constexpr int D = OpTraits<OP>::kDim;
   constexpr bool LOG = (OP == SKF_LAPLACE_2D);
   constexpr int TS = symw_ts();
@@ -1172,9 +1172,9 @@ __global__ void __launch_bounds__(kSymwWarps * 32, 3) k_translate_symw(SymArgs a
   float* sTu = reinterpret_cast<float*>(sbuf + 2 * 4 * TS);  // [TS][33]
   float* sTh = sTu + TS * 33;
 
-  const int U = a.work_box[blockIdx.x];
-  const int row0 = a.work_row[blockIdx.x];
-  const int part = a.work_part[blockIdx.x];
+  const int U = a.work_box[item];
+  const int row0 = a.work_row[item];
+  const int part = a.work_part[item];
   const int64_t offU = a.box_off[U];
   const int bsU = (int)(a.box_off[U + 1] - offU);
   const int rU = a.box_rank[U];
@@ -1373,6 +1373,30 @@ __global__ void __launch_bounds__(kSymwWarps * 32, 3) k_translate_symw(SymArgs a
       apart[2 * bsU + row] = (float)(vu - (double)hu);
       apart[3 * bsU + row] = (float)(vh - (double)hh);
     }
+  }
+}
+
+// One block per item of the (costliest-first) item list.
+template <int OP>
+__global__ void __launch_bounds__(kSymwWarps * 32, 3) k_translate_symw(SymArgs a) {
+  symw_item<OP>(a, blockIdx.x);
+}
+
+// Persistent form: one block per resident slot (3 per SM) takes items from
+// a queue counter (zeroed before the launch) in list order until it is
+// exhausted.  Which block takes an item changes from run to run; what an
+// item writes (its rows, its partial slots) does not, so results are the
+// same bit for bit.
+template <int OP>
+__global__ void __launch_bounds__(kSymwWarps * 32, 3) k_translate_symw_queue(SymArgs a, int nitems, int* queue) {
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();  // all threads read s_item (and finished the last item) first
+    if (item >= nitems) break;
+    symw_item<OP>(a, item);
   }
 }
 

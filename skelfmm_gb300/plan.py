@@ -318,7 +318,8 @@ class Plan:
         self.set_option(_lib.OPT_SYMMETRIC, 1)
         info = self._query()
         sym_ok = info.npairs_evaluated_mixed < info.npairs_fused
-        nsym = 4 if self.is_complex else 5  # shape 4: the source-split Laplace kernel
+        # shapes 4 and 5: the source-split Laplace kernel (grid, persistent queue)
+        nsym = 4 if self.is_complex else 6
         cands = ([(1, sh) for sh in range(nsym)] if sym_ok else []) + [(0, sh) for sh in range(3)]
         results = {}
         for sym, shape in cands:

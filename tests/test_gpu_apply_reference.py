@@ -117,14 +117,14 @@ def test_symmetric_translations_agree(name):
 @pytest.mark.parametrize("name", ["lap3d_cube", "lap3d_c2params", "lap2d_annulus", "helm3d_sphere"])
 def test_symmetric_tile_shapes_agree(name):
     """Every tile shape of the symmetric kernel (sources per tile, blocks per
-    SM, and the source-split kernel) gives the same apply up to the order of
-    the partial sums; each is deterministic."""
+    SM, and the source-split kernel on a grid or a persistent queue) gives the
+    same apply up to the order of the partial sums; each is deterministic."""
     from skelfmm_gb300 import _lib
 
     d, plan = _plan(name)
     x = np.ascontiguousarray(d["x"])
     ys = []
-    for shape in range(5):
+    for shape in range(6):
         plan.set_option(_lib.OPT_SYM_SHAPE, shape)
         y = np.empty_like(x)
         plan.apply_host(x, y, _lib.PREC_MIXED)

@@ -39,11 +39,14 @@ def test_mlp_gradient_matches_oracle():
     theta16, X16 = _oracle_inputs(m, X)
     lo, go = M.loss_and_grad(theta16, X16, y, NIN, bf16=True)
     assert abs(loss - lo) <= 1e-3 * lo
-    # per-block relative error (BF16 activations may round differently at a
-    # few ties when the FP32 sums are taken in another order)
-    assert np.linalg.norm(g - go) <= 2e-2 * np.linalg.norm(go)
-    W1 = slice(0, 128 * NIN)
-    assert np.linalg.norm(g[W1] - go[W1]) <= 2e-2 * np.linalg.norm(go[W1])
+    # every parameter block (W1 b1 W2 b2 w3 b3) to 1e-5 relative: the oracle
+    # rounds the activations to BF16 where the kernels do, so only the order
+    # of the FP32 sums differs (the FP32-activation gradient differs from
+    # both by ~1e-2 in W1)
+    H = 128
+    ends = np.cumsum([0, H * NIN, H, H * H, H, H, 1])
+    for a, b in zip(ends[:-1], ends[1:]):
+        assert np.linalg.norm(g[a:b] - go[a:b]) <= 1e-5 * np.linalg.norm(go[a:b]), (a, b)
 
 
 def test_mlp_predict_matches_oracle():
