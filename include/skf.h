@@ -270,6 +270,18 @@ int skf_mlp_train_step(int32_t nin, float* theta, void* theta16, const void* x16
 int skf_box_moments(int32_t nbox, int32_t ndim, const int64_t* off, const double* x, const double* centers,
                     double width, double* out, void* stream);
 
+/*
+ * Point-level front end of the tree build (the tree the reference takes from
+ * simpletree.BalancedTree, called at skelfmm/skel_fmm.py:150): for point i
+ * of x [n x ndim] (DEVICE, FP64) the integer cell q[i, d] = clamp(floor((x -
+ * corner[d]) / L0 * 2^depth), 0, 2^depth - 1) of the root box's finest grid
+ * and keys[i], its bit interleave (axis 0 most significant in every
+ * ndim-bit group).  corner: DEVICE [ndim]; q may be NULL.  ndim 2 or 3,
+ * depth * ndim <= 63.
+ */
+int skf_morton_keys(int32_t ndim, int64_t n, const double* x, const double* corner, double L0, int32_t depth,
+                    uint64_t* keys, int64_t* q, void* stream);
+
 const char* skf_status_string(int32_t status);
 int skf_version(void);
 

@@ -14,7 +14,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libskf.so")
-SOURCES = ["skf_apply.cu", "skf_build.cu", "skf_capi.cu", "skf_noalloc.cu", "skf_mlp.cu"]
+SOURCES = ["skf_apply.cu", "skf_build.cu", "skf_capi.cu", "skf_noalloc.cu", "skf_mlp.cu", "skf_tree.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(REPO, "include")]
 

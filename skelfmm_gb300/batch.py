@@ -100,7 +100,7 @@ class SkelFMMBatch:
         self.sizes = [int(p.shape[0]) for p in point_sets]
         rbs = []
         for i, pts in enumerate(self.point_sets):
-            tree = BalancedTree(pts, leaf_size)
+            tree = BalancedTree(pts, leaf_size, device="cuda")
             fmm = RecursiveSkeletonization(tree, operator, param, tol,
                                            geometry=None if geometries is None else geometries[i])
             fmm.skel_tree(npoints_max=npoints_max)

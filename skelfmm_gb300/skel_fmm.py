@@ -170,7 +170,7 @@ class SkelFMM:
                 stack.enter_context(contextlib.redirect_stdout(io.StringIO()))
                 stack.enter_context(contextlib.redirect_stderr(io.StringIO()))
             t0 = perf_counter()
-            self.tree = BalancedTree(self.points, leaf_size=self.leaf_size)
+            self.tree = BalancedTree(self.points, leaf_size=self.leaf_size, device=self.device)
             self.tree_time_seconds = perf_counter() - t0
             self.nlevels = self.tree.nlevels
             self.nboxes = self.tree.nboxes

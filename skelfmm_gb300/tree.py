@@ -84,7 +84,12 @@ def findin_sorted(arr, val):
 class BalancedTree:
     """Adaptive, 2:1-balanced tree over ``points[N, d]`` (d = 2 or 3)."""
 
-    def __init__(self, points, leaf_size):
+    def __init__(self, points, leaf_size, device=None):
+        """``device``: a CUDA device (torch.device or string) to compute the
+        point-level front end there (the points' integer cells and Morton
+        keys in a CUDA kernel, the stable key sort on the device); the box
+        levels are then refined on the host as without it, and the tree is
+        identical."""
         XX = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
         if XX.ndim != 2 or XX.shape[1] not in (2, 3):
             raise ValueError("points must have shape (N, 2) or (N, 3)")
@@ -97,36 +102,38 @@ class BalancedTree:
         self.leaf_size = int(leaf_size)
         ndim = self.ndim
 
-        lo = XX.min(axis=0)
-        hi = XX.max(axis=0)
-        self.c0 = 0.5 * (lo + hi)
-        ext = float(np.max(hi - lo))
-        self.L0 = ext if ext > 0 else 1.0
-
         D = _MAX_DEPTH[ndim]
         self._depth = D
-        corner = self.c0 - 0.5 * self.L0
-        # (x - corner) / L0 * 2^D, floored and clipped to [0, 2^D - 1], in place
-        scaled = XX - corner[None, :]
-        scaled /= self.L0
-        scaled *= float(1 << D)
-        np.floor(scaled, out=scaled)
-        np.minimum(scaled, float((1 << D) - 1), out=scaled)
-        np.maximum(scaled, 0.0, out=scaled)
-        q = scaled.astype(np.int64)
-        del scaled
-        keys = morton_encode(q, D)
-        # stable argsort: an unstable sort, then input order restored among
-        # equal keys (points sharing a finest cell; rare)
-        perm = np.argsort(keys)
-        skeys = keys[perm]
-        tie = np.flatnonzero(skeys[1:] == skeys[:-1])
-        if tie.size:
-            pos = np.unique(np.concatenate((tie, tie + 1)))
-            perm[pos] = perm[pos][np.lexsort((perm[pos], skeys[pos]))]
-        self._perm = perm
-        self._skeys = skeys
-        self._q = q  # integer coordinates in input order (box corners via _perm)
+        if device is not None and str(device).startswith("cuda"):
+            self._front_end_device(XX, device)
+        else:
+            lo = XX.min(axis=0)
+            hi = XX.max(axis=0)
+            self.c0 = 0.5 * (lo + hi)
+            ext = float(np.max(hi - lo))
+            self.L0 = ext if ext > 0 else 1.0
+            corner = self.c0 - 0.5 * self.L0
+            # (x - corner) / L0 * 2^D, floored and clipped to [0, 2^D - 1], in place
+            scaled = XX - corner[None, :]
+            scaled /= self.L0
+            scaled *= float(1 << D)
+            np.floor(scaled, out=scaled)
+            np.minimum(scaled, float((1 << D) - 1), out=scaled)
+            np.maximum(scaled, 0.0, out=scaled)
+            q = scaled.astype(np.int64)
+            del scaled
+            keys = morton_encode(q, D)
+            # stable argsort: an unstable sort, then input order restored among
+            # equal keys (points sharing a finest cell; rare)
+            perm = np.argsort(keys)
+            skeys = keys[perm]
+            tie = np.flatnonzero(skeys[1:] == skeys[:-1])
+            if tie.size:
+                pos = np.unique(np.concatenate((tie, tie + 1)))
+                perm[pos] = perm[pos][np.lexsort((perm[pos], skeys[pos]))]
+            self._perm = perm
+            self._skeys = skeys
+            self._q = q  # integer coordinates in input order (box corners via _perm)
 
         # per level (sorted by Morton code): coords, codes, point ranges, leaf flags
         self._Lc = [np.zeros((1, ndim), dtype=np.int64)]
@@ -150,6 +157,35 @@ class BalancedTree:
         self._finalize()
 
     # ------------------------------------------------------------------ build
+    def _front_end_device(self, XX, device):
+        """Root box, integer cells, keys and the stable key order computed on
+        ``device``: skf_morton_keys (the same FP64 steps as the host path)
+        and a stable device sort (ties keep the input order)."""
+        import torch
+
+        from . import _lib
+
+        dev = torch.device(device)
+        x = torch.from_numpy(XX).to(dev)
+        lo, hi = torch.aminmax(x, dim=0)
+        lo, hi = lo.cpu().numpy(), hi.cpu().numpy()
+        self.c0 = 0.5 * (lo + hi)
+        ext = float(np.max(hi - lo))
+        self.L0 = ext if ext > 0 else 1.0
+        corner = self.c0 - 0.5 * self.L0
+        n, ndim = XX.shape
+        ct = torch.from_numpy(np.ascontiguousarray(corner)).to(dev)
+        keys = torch.empty(n, dtype=torch.int64, device=dev)
+        q = torch.empty((n, ndim), dtype=torch.int64, device=dev)
+        _lib.check(_lib.load().skf_morton_keys(ndim, n, _lib.ptr(x), _lib.ptr(ct), float(self.L0), self._depth,
+                                                _lib.ptr(keys), _lib.ptr(q),
+                                                torch.cuda.current_stream(dev).cuda_stream), "skf_morton_keys")
+        # keys < 2^63: the signed order is the unsigned one
+        skeys, perm = torch.sort(keys, stable=True)
+        self._perm = perm.cpu().numpy()
+        self._skeys = skeys.cpu().numpy().view(np.uint64)
+        self._q = q.cpu().numpy()
+
     def _lookup(self, lev, coords):
         """Index within level ``lev`` of the boxes at integer ``coords``, -1 if absent."""
         n = self._Lk[lev].shape[0]
