@@ -333,28 +333,34 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
     auto mirror = [](int k) {
       return k == SKF_KIND_COARSE_UP ? SKF_KIND_COARSE_DOWN : (k == SKF_KIND_COARSE_DOWN ? SKF_KIND_COARSE_UP : k);
     };
-    std::unordered_map<uint64_t, int> seen;
-    seen.reserve((size_t)L * 2);
+    // each box's list sorted by source: no source twice, and every (A, B,
+    // kind) has its (B, A, mirror kind) in B's list (binary search)
+    std::vector<std::pair<int32_t, int8_t>> sorted_lists((size_t)L);
+    for (int64_t l = 0; l < L; ++l) sorted_lists[l] = {d->list_src[l], d->list_kind[l]};
     bool ok = true;
-    for (int A = 0; A < nb && ok; ++A)
-      for (int64_t l = d->list_off[A]; l < d->list_off[A + 1]; ++l) {
-        const int B = d->list_src[l];
-        if (B == A) continue;
-        const uint64_t key = (uint64_t)A * (uint64_t)nb + (uint64_t)B;
-        if (seen.count(key)) { ok = false; break; }
-        seen[key] = d->list_kind[l];
-      }
-    for (auto it = seen.begin(); ok && it != seen.end(); ++it) {
-      const uint64_t A = it->first / (uint64_t)nb, B = it->first % (uint64_t)nb;
-      auto m = seen.find(B * (uint64_t)nb + A);
-      if (m == seen.end() || m->second != mirror(it->second)) ok = false;
+    for (int A = 0; A < nb && ok; ++A) {
+      auto b = sorted_lists.begin() + d->list_off[A], e = sorted_lists.begin() + d->list_off[A + 1];
+      std::sort(b, e);
+      for (auto it = b; it + 1 < e; ++it)
+        if (it->first == (it + 1)->first) ok = false;
     }
+    for (int A = 0; A < nb && ok; ++A)
+      for (int64_t l = d->list_off[A]; l < d->list_off[A + 1] && ok; ++l) {
+        const int B = sorted_lists[l].first;
+        if (B == A) continue;
+        auto b = sorted_lists.begin() + d->list_off[B], e = sorted_lists.begin() + d->list_off[B + 1];
+        auto m = std::lower_bound(b, e, std::make_pair((int32_t)A, (int8_t)INT8_MIN));
+        if (m == e || m->first != A || m->second != mirror(sorted_lists[l].second)) ok = false;
+      }
+    std::vector<std::pair<int32_t, int8_t>>().swap(sorted_lists);
     if (ok) {
       const int tile = kT32Threads * kRowsPerThreadF32;
       std::vector<int64_t> soff(nb + 1, 0), poff, pbase(nb, 0), pstride(nb, 0);
       std::vector<int32_t> ssrc;
       std::vector<int8_t> skind;
-      std::vector<std::vector<int64_t>> incoming(nb);
+      // B-side partial blocks each box receives, as (box, block) in the
+      // order the reduction adds them, grouped into CSR below
+      std::vector<std::pair<int32_t, int64_t>> incoming;
       int64_t total = 0, sym_pairs = 0;
       std::vector<std::pair<int64_t, std::pair<int32_t, int32_t>>> items;
       for (int A = 0; A < nb; ++A) {
@@ -377,7 +383,7 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
         const int64_t ntiles = bsA > 0 ? (bsA + tile - 1) / tile : 0;
         for (int64_t t = 0; t < ntiles; ++t)
           for (size_t k = first; k < ssrc.size(); ++k)
-            if (ssrc[k] != A) incoming[ssrc[k]].push_back(total + t * stride + poff[k]);
+            if (ssrc[k] != A) incoming.push_back({ssrc[k], total + t * stride + poff[k]});
         total += ntiles * stride;
         sym_pairs += bsA * srcsum;
         if (bsA > 0 && ssrc.size() > first)
@@ -390,11 +396,18 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
         wb[i] = items[i].second.first;
         wr[i] = items[i].second.second;
       }
-      std::vector<int64_t> ioff(nb + 1, 0), iblk;
-      for (int B = 0; B < nb; ++B) {
-        ioff[B + 1] = ioff[B] + (int64_t)incoming[B].size();
-        iblk.insert(iblk.end(), incoming[B].begin(), incoming[B].end());
-      }
+      // CSR by receiving box, keeping the order within each box (counting sort)
+      auto to_csr = [nb](const std::vector<std::pair<int32_t, int64_t>>& in, std::vector<int64_t>& off,
+                         std::vector<int64_t>& blk) {
+        off.assign((size_t)nb + 1, 0);
+        for (const auto& e : in) ++off[(size_t)e.first + 1];
+        for (int B = 0; B < nb; ++B) off[B + 1] += off[B];
+        blk.resize(in.size());
+        std::vector<int64_t> fill(off.begin(), off.end() - 1);
+        for (const auto& e : in) blk[fill[e.first]++] = e.second;
+      };
+      std::vector<int64_t> ioff, iblk;
+      to_csr(incoming, ioff, iblk);
       SKF_TRY(upload(p, &p->sym_list_off, soff.data(), soff.size()));
       SKF_TRY(upload(p, &p->sym_list_src, ssrc.data(), std::max<size_t>(ssrc.size(), 1)));
       SKF_TRY(upload(p, &p->sym_list_kind, skind.data(), std::max<size_t>(skind.size(), 1)));
@@ -429,7 +442,7 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
       // an even share for ~4 waves of 3 blocks per SM on 152 SMs
       const double share = (double)wcost_total / (152.0 * 3.0 * 4.0);
       int64_t aoff = total;
-      std::vector<std::vector<int64_t>> incoming_w = incoming;
+      std::vector<std::pair<int32_t, int64_t>> incoming_w = std::move(incoming);
       std::vector<std::pair<int64_t, std::array<int32_t, 3>>> witems;
       for (int A = 0; A < nb && !cplx; ++A) {
         const int64_t bsA = d->box_off[A + 1] - d->box_off[A];
@@ -442,8 +455,8 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
           apart[A] = aoff;
           for (int q = 1; q < P; ++q) {
             // hi and lo halves of the part's row sums: two incoming blocks
-            incoming_w[A].push_back(aoff + (int64_t)(q - 1) * 4 * bsA);
-            incoming_w[A].push_back(aoff + (int64_t)(q - 1) * 4 * bsA + 2 * bsA);
+            incoming_w.push_back({A, aoff + (int64_t)(q - 1) * 4 * bsA});
+            incoming_w.push_back({A, aoff + (int64_t)(q - 1) * 4 * bsA + 2 * bsA});
           }
           aoff += (int64_t)(P - 1) * 4 * bsA;
         }
@@ -459,11 +472,8 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
         wwr[i] = witems[i].second[1];
         wwq[i] = witems[i].second[2];
       }
-      std::vector<int64_t> ioffw(nb + 1, 0), iblkw;
-      for (int B = 0; B < nb; ++B) {
-        ioffw[B + 1] = ioffw[B] + (int64_t)incoming_w[B].size();
-        iblkw.insert(iblkw.end(), incoming_w[B].begin(), incoming_w[B].end());
-      }
+      std::vector<int64_t> ioffw, iblkw;
+      to_csr(incoming_w, ioffw, iblkw);
       total = aoff;
       SKF_TRY(upload(p, &p->box_ntiles, ntil.data(), ntil.size()));
       SKF_TRY(upload(p, &p->box_nparts, npart.data(), npart.size()));
