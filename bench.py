@@ -15,11 +15,12 @@ Multi-GPU runs are independent replicas (one instance per rank, no
 collective on the data path); ``value`` sums all ranks.
 ``--impl reference`` times the reference algorithm's CPU implementation (the
 oracle port of skelfmm's batched apply) on all host cores, on the same config:
-complete applies when they are short, otherwise each step times a random
-sample of the apply's kernel blocks (drawn in proportion to their work) and
-the apply time is estimated from the sampled rate; the estimate is checked
-against a complete apply (``calibration``).  The GPU arm's ``cpu_baseline``
-uses the same estimator.
+complete applies when they are short; otherwise each step times a random
+sample of the apply's kernel blocks (drawn in proportion to their work), and
+one complete apply gives the apply time when it takes under a minute (the
+sampled estimate is reported beside it as ``calibration``), else the sampled
+estimate does, checked against a complete apply of a smaller instance.  The
+GPU arm's ``cpu_baseline`` uses the same function with one step.
 
 Other workloads (``--workload``): ``laplace2d_square_100k`` (2D Laplace,
 N = 1e5 uniform in [0,1]^2, tol 1e-5, leaf 200), ``helmholtz3d_sphere_2M``
@@ -84,6 +85,9 @@ def parse():
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--ncheck", type=int, default=2000)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    # keep the plan's default translation scheme instead of timing the
+    # candidates (profiling runs, where ncu's serialisation skews the timings)
+    p.add_argument("--no-autotune", action="store_true")
     return p.parse_args()
 
 
@@ -318,10 +322,15 @@ CAL_N = {"cube": 100_000, "sphere_surface": 100_000, "square": 100_000}
 
 
 def reference_baseline(cfg, point_sets, xs, ncores, steps, warmup, calibrate=True):
-    """The reference algorithm on the host cores for a workload: complete
-    applies when they are short, otherwise the sampled estimate, checked
-    against a complete apply (of the workload itself when one is short, else
-    of a smaller instance of the same workload)."""
+    """The reference algorithm on the host cores for a workload.
+
+    * Complete applies are timed when ``warmup + steps`` of them take under
+      90 s (from a one-step sampled estimate).
+    * Otherwise each step times a sampled set of kernel blocks; when one
+      complete apply takes under 60 s it is also timed and gives the
+      reported apply time (the sampled estimate is reported beside it);
+      otherwise the sampled estimate is reported and checked against a
+      complete apply of a smaller instance of the workload."""
     t0 = time.perf_counter()
     builds = oracle_builds(point_sets, cfg["opname"], cfg["kappa"], cfg["tol"], cfg["leaf"], ncores)
     build_s = time.perf_counter() - t0
@@ -336,19 +345,22 @@ def reference_baseline(cfg, point_sets, xs, ncores, steps, warmup, calibrate=Tru
                    sample=f"{steps} complete applies, FP64 numpy dense kernel blocks")
         return out
     est = ra.sampled(steps, warmup, REF_STEP_EVALS)
-    if calibrate and probe["apply_s"] < 60.0:
+    desc = (f"{steps} steps x {est['blocks_per_step']} kernel blocks (~{est['step_evals']:.2g} evaluations) "
+            f"drawn in proportion to the apply's blocks, largest first ({100 * est['sampled_evals'] / ra.total:.2f}% "
+            f"of one apply in all), FP64 numpy dense kernel blocks")
+    if probe["apply_s"] < 60.0:
         t_full = ra.full()
+        out.update(kind="complete apply + sampled steps", apply_s=t_full, step_s=est["step_s"],
+                   sample=f"one complete apply ({t_full:.1f} s) gives the apply time; {desc}")
         out["calibration"] = {"N": ra.npoints, "complete_apply_s": round(t_full, 3),
                               "sampled_estimate_s": round(est["apply_s"], 3),
                               "estimate_over_complete": round(est["apply_s"] / t_full, 3)}
-    elif calibrate:
-        out["calibration"] = reference_calibration(cfg, ncores)
+        return out
     out.update(kind="sampled", apply_s=est["apply_s"], step_s=est["step_s"],
-               sample=f"{steps} steps x {est['blocks_per_step']} kernel blocks (~{est['step_evals']:.2g} "
-                      f"evaluations) drawn in proportion to the apply's blocks, largest first "
-                      f"({100 * est['sampled_evals'] / ra.total:.2f}% of one apply in all), "
-                      f"FP64 numpy dense kernel blocks; apply time = upward + downward passes "
-                      f"({est['up_s'] + est['down_s']:.2f} s, timed in full) + evaluations / sampled rate")
+               sample=f"{desc}; apply time = upward + downward passes ({est['up_s'] + est['down_s']:.2f} s, timed "
+                      f"in full) + evaluations / sampled rate")
+    if calibrate:
+        out["calibration"] = reference_calibration(cfg, ncores)
     return out
 
 
@@ -406,7 +418,8 @@ def roofline_line(plan, t_ms, opname, traffic_name):
     ops_pair = ops_per_eval(opname, False)
     ops_eval = ops_per_eval(opname, sym)
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    tuned = tuple(getattr(plan, "tuned", (1 if sym else 0, 0)))
+    default = (1, 4 if opname.startswith("laplace") else 0) if sym else (0, 0)  # the plan's defaults
+    tuned = tuple(getattr(plan, "tuned", default))
     opu = opname.upper()
     kern = (KERNEL_NAMES.get(tuned, "k_translate_sym<{op}> + k_sym_reduce").format(op=opu) if sym else
             (f"k_translate_f32x2<{opu}>" if opname.startswith("laplace") else
@@ -453,7 +466,8 @@ def run_single(args):
     SkelFMM(pts[:20000], op, tol=cfg["tol"], leaf_size=cfg["leaf"], param=cfg["kappa"], precision="mixed")
     barrier()
     t0 = time.perf_counter()
-    f = SkelFMM(pts, op, tol=cfg["tol"], leaf_size=cfg["leaf"], param=cfg["kappa"], precision="mixed")
+    f = SkelFMM(pts, op, tol=cfg["tol"], leaf_size=cfg["leaf"], param=cfg["kappa"], precision="mixed",
+                autotune=not args.no_autotune)
     torch.cuda.synchronize(dev)
     build_s = time.perf_counter() - t0
     plan = f.plan
@@ -518,7 +532,7 @@ def run_single(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         ncores = os.cpu_count() or 1
-        res = reference_baseline(cfg, [pts], [x], ncores, steps=4, warmup=1, calibrate=False)
+        res = reference_baseline(cfg, [pts], [x], ncores, steps=1, warmup=0, calibrate=False)
         cpu = {"value": round(res["npoints"] / res["apply_s"] / 1e6, 6), "unit": "Mpts/s", "cores": ncores,
                "kind": "port", "sample": res["sample"]}
     value = n * ws / (ms_step * 1e-3) / 1e6
@@ -619,7 +633,7 @@ def run_batch(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         ncores = os.cpu_count() or 1
-        res = reference_baseline(BATCH_CFG, pts, xs, ncores, steps=4, warmup=1, calibrate=False)
+        res = reference_baseline(BATCH_CFG, pts, xs, ncores, steps=1, warmup=0, calibrate=False)
         cpu = {"value": round(res["npoints"] / res["apply_s"] / 1e6, 6), "unit": "Mpts/s", "cores": ncores,
                "kind": "port", "sample": res["sample"]}
     # ranks hold different instances: the job's units are summed over ranks

@@ -86,7 +86,7 @@ class SkelFMM:
     def __init__(self, points, operator, geometry=None, tol=1e-5, rank_or_tol=None, leaf_size=200,
                  use_single_precision=False, param=0.0, quiet=True, keep_host_fmm=False, defer_build=False,
                  npoints_max=500, p="auto", max_bs=-1, max_rank=-1, precision=None, learned_rank=False,
-                 cuda_graph=False):
+                 cuda_graph=False, autotune=True):
         self.points = np.asarray(points, dtype=np.float64)
         if self.points.ndim != 2 or not np.all(np.isfinite(self.points)):
             raise ValueError("points must be a finite [N, ndim] array")
@@ -130,6 +130,9 @@ class SkelFMM:
         # cuda_graph: record one apply of the built operator into a CUDA graph
         # (capture()); applies then replay it on static device buffers
         self._cuda_graph = bool(cuda_graph)
+        # autotune: time the translation schemes after the build and keep the
+        # fastest (mixed precision); False keeps the plan's default scheme
+        self._autotune = bool(autotune)
         self._graph = None
         self._gx = self._gy = None
         self.device = torch.device("cuda") if torch.cuda.is_available() else None
@@ -191,7 +194,7 @@ class SkelFMM:
             fmm.setup_lists(verbose=verbose)
             self.plan = Plan(fmm.ragged())
             self.tuning = None
-            if self._prec_code != _lib.PREC_FP64:
+            if self._prec_code != _lib.PREC_FP64 and self._autotune:
                 # translation scheme and tile shape for this plan, by timing them
                 self.tuning = self.plan.autotune(self._prec_code, reps=2)
             torch.cuda.synchronize(self.device)

@@ -36,6 +36,8 @@ import itertools
 import numpy as np
 
 _MAX_DEPTH = {2: 30, 3: 20}
+# below this many points the host front end is faster than the device round trip
+DEVICE_FRONT_END_MIN_POINTS = 100_000
 
 
 def _spread_bits(v: np.ndarray, ndim: int, nbits: int) -> np.ndarray:
@@ -86,10 +88,10 @@ class BalancedTree:
 
     def __init__(self, points, leaf_size, device=None):
         """``device``: a CUDA device (torch.device or string) to compute the
-        point-level front end there (the points' integer cells and Morton
-        keys in a CUDA kernel, the stable key sort on the device); the box
-        levels are then refined on the host as without it, and the tree is
-        identical."""
+        point-level front end there for clouds of DEVICE_FRONT_END_MIN_POINTS
+        or more (the points' integer cells and Morton keys in a CUDA kernel,
+        the stable key sort on the device); the box levels are then refined
+        on the host as without it, and the tree is identical."""
         XX = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
         if XX.ndim != 2 or XX.shape[1] not in (2, 3):
             raise ValueError("points must have shape (N, 2) or (N, 3)")
@@ -104,7 +106,7 @@ class BalancedTree:
 
         D = _MAX_DEPTH[ndim]
         self._depth = D
-        if device is not None and str(device).startswith("cuda"):
+        if device is not None and str(device).startswith("cuda") and self.N >= DEVICE_FRONT_END_MIN_POINTS:
             self._front_end_device(XX, device)
         else:
             lo = XX.min(axis=0)

@@ -28,8 +28,16 @@ def _same(a, b):
 def test_device_front_end_gives_the_host_tree_on_golden_points(name):
     from skelfmm_gb300.tree import BalancedTree
 
+    from skelfmm_gb300 import tree as T
+
     d = load_build(name)
-    _same(BalancedTree(d["points"], int(d["leaf_size"])), BalancedTree(d["points"], int(d["leaf_size"]), device="cuda"))
+    saved = T.DEVICE_FRONT_END_MIN_POINTS
+    T.DEVICE_FRONT_END_MIN_POINTS = 1  # the golden sets are smaller than the threshold
+    try:
+        b = BalancedTree(d["points"], int(d["leaf_size"]), device="cuda")
+    finally:
+        T.DEVICE_FRONT_END_MIN_POINTS = saved
+    _same(BalancedTree(d["points"], int(d["leaf_size"])), b)
 
 
 def test_device_front_end_on_4e6_clustered_points():
@@ -38,7 +46,7 @@ def test_device_front_end_on_4e6_clustered_points():
     pts = get_point_dist(4_000_000, "gaussian_clusters", rng=np.random.default_rng(0))
     # coincident points (ties in the finest cell) keep their input order
     pts[1000:1010] = pts[5]
-    BalancedTree(pts[:1000], 256, device="cuda")  # first use of the kernels
+    BalancedTree(pts[:200000], 256, device="cuda")  # first use of the kernels
     t0 = time.perf_counter()
     a = BalancedTree(pts, 256)
     t1 = time.perf_counter()
