@@ -496,8 +496,9 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
             c.work_box = p->worksymw.box;
             c.work_row = p->worksymw.row;
             if (p->worksymw.n > 0) launch_symw<OP>(c, p->worksymw.n, p->sym_shape == 5 ? p->symw_queue : nullptr, st);
-            k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
-                p->box_off, p->box_rank, p->in_off_w, p->in_blk_w, p->pbuf, p->u, p->uh);
+            if (p->red.n > 0)
+              k_sym_reduce<OP == SKF_LAPLACE_2D><<<p->red.n, 256, 0, st>>>(
+                  p->red.box, p->red.row, p->box_off, p->box_rank, p->in_off_w, p->in_blk_w, p->pbuf, p->u, p->uh);
           } else {
             if (p->worksym.n > 0) {
               // tile shape: 0 = 64 sources, 5 blocks/SM; 1 = 128 sources, 3 blocks/SM;
@@ -509,8 +510,9 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
                 default: launch_sym<OP, 64, 5>(c, p->worksym.n, st); break;
               }
             }
-            k_sym_reduce<OP == SKF_LAPLACE_2D><<<dim3(p->nboxes, (p->max_bs + 255) / 256), 256, 0, st>>>(
-                p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
+            if (p->red.n > 0)
+              k_sym_reduce<OP == SKF_LAPLACE_2D><<<p->red.n, 256, 0, st>>>(
+                  p->red.box, p->red.row, p->box_off, p->box_rank, p->in_off, p->in_blk, p->pbuf, p->u, p->uh);
           }
           return;
         }

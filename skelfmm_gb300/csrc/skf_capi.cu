@@ -481,6 +481,24 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
       SKF_TRY(upload(p, &p->in_off_w, ioffw.data(), ioffw.size()));
       if (!iblkw.empty()) SKF_TRY(upload(p, &p->in_blk_w, iblkw.data(), iblkw.size()));
       SKF_TRY(upload(p, &p->symw_queue, (const int*)nullptr, 1));
+      {
+        // reduction items: 256-entry chunks of the boxes that receive partials
+        // (under either scheme's lists)
+        std::vector<int32_t> rb, rc;
+        for (int B = 0; B < nb; ++B) {
+          const int64_t bsB = d->box_off[B + 1] - d->box_off[B];
+          if (bsB == 0 || (ioff[B + 1] == ioff[B] && ioffw[B + 1] == ioffw[B])) continue;
+          for (int64_t c = 0; c * 256 < bsB; ++c) {
+            rb.push_back(B);
+            rc.push_back((int32_t)c);
+          }
+        }
+        p->red.n = (int)rb.size();
+        if (p->red.n > 0) {
+          SKF_TRY(upload(p, &p->red.box, rb.data(), rb.size()));
+          SKF_TRY(upload(p, &p->red.row, rc.data(), rc.size()));
+        }
+      }
       p->worksymw.n = (int)witems.size();
       if (p->worksymw.n > 0) {
         SKF_TRY(upload(p, &p->worksymw.box, wwb.data(), wwb.size()));

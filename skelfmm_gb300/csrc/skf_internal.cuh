@@ -109,6 +109,7 @@ struct skf_plan {
   int32_t* list_src = nullptr;
   int8_t* list_kind = nullptr;
   skf::WorkList work64, work32, worksym, worksymw;
+  skf::WorkList red;  // partial reduction items: box, 256-entry chunk (in .row)
   std::vector<skf::LevelBoxes> levels;  // indexed by level
   // apply vectors (scalars; complex: 2 doubles per entry)
   double* q = nullptr;

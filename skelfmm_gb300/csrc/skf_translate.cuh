@@ -1780,42 +1780,56 @@ __global__ void __launch_bounds__(256) k_sym_reduce_c(const int64_t* __restrict_
   }
 }
 
-// Adds the B-side partial sums into u / uh in a fixed order.  Block
-// (box, chunk): entries [256 chunk, 256 chunk + 256) of the box.
+// Adds the B-side partial sums into u / uh in a fixed order.  Block i of the
+// launch takes item (box, chunk) = (red_box[i], red_chunk[i]): entries
+// [256 chunk, 256 chunk + 256) of a box that receives partials (the plan
+// lists only those); uh partials are read only for skeleton entries.
 template <bool LOG>
-__global__ void __launch_bounds__(256) k_sym_reduce(const int64_t* __restrict__ box_off,
+__global__ void __launch_bounds__(256) k_sym_reduce(const int32_t* __restrict__ red_box,
+                                                    const int32_t* __restrict__ red_chunk,
+                                                    const int64_t* __restrict__ box_off,
                                                     const int32_t* __restrict__ box_rank,
                                                     const int64_t* __restrict__ in_off,
                                                     const int64_t* __restrict__ in_blk,
                                                     const float* __restrict__ pbuf, double* __restrict__ u,
                                                     double* __restrict__ uh) {
-  const int B = blockIdx.x;
+  const int B = red_box[blockIdx.x];
   const int64_t off = box_off[B];
   const int bs = (int)(box_off[B + 1] - off);
-  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  const int j = red_chunk[blockIdx.x] * blockDim.x + threadIdx.x;
   const int64_t k0 = in_off[B], k1 = in_off[B + 1];
   if (j >= bs || k0 == k1) return;
   const int r = box_rank[B];
+  const bool skel = j < r;
   const double scale = LOG ? 0.34657359027997264 : 1.0;
   // four independent chains keep eight loads in flight per thread; the
   // grouping is fixed, so the sum is deterministic
-  double su[4] = {0.0, 0.0, 0.0, 0.0}, sh[4] = {0.0, 0.0, 0.0, 0.0};
+  // four chains of compensated FP32 sums (TwoSum: value and rounding error,
+  // ~2^-48 relative, as an FP64 sum; the FP32 pipes instead of the FP64 pipe)
+  float su[4] = {0.f, 0.f, 0.f, 0.f}, cu[4] = {0.f, 0.f, 0.f, 0.f};
+  float sh[4] = {0.f, 0.f, 0.f, 0.f}, ch[4] = {0.f, 0.f, 0.f, 0.f};
   int64_t k = k0;
   for (; k + 3 < k1; k += 4) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int64_t b = in_blk[k + q];
-      su[q] += (double)pbuf[b + j];
-      sh[q] += (double)pbuf[b + bs + j];
+      two_sum_add(su[q], cu[q], pbuf[b + j]);
+      if (skel) two_sum_add(sh[q], ch[q], pbuf[b + bs + j]);
     }
   }
   for (int q = 0; k < k1; ++k, ++q) {
     const int64_t b = in_blk[k];
-    su[q] += (double)pbuf[b + j];
-    sh[q] += (double)pbuf[b + bs + j];
+    two_sum_add(su[q], cu[q], pbuf[b + j]);
+    if (skel) two_sum_add(sh[q], ch[q], pbuf[b + bs + j]);
   }
-  u[off + j] += scale * ((su[0] + su[1]) + (su[2] + su[3]));
-  if (j < r) uh[off + j] += scale * ((sh[0] + sh[1]) + (sh[2] + sh[3]));
+  double vu = 0.0, vh = 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    vu += (double)su[q] + (double)cu[q];
+    vh += (double)sh[q] + (double)ch[q];
+  }
+  u[off + j] += scale * vu;
+  if (skel) uh[off + j] += scale * vh;
 }
 
 }  // namespace skf
