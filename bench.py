@@ -439,7 +439,7 @@ def roofline_line(plan, t_ms, opname, traffic_name):
     }
 
 
-TRAFFIC_PROFILE = {"laplace3d_cube_1M": "translate_sym_lap3d_1M.md"}  # per-launch DRAM bytes from ncu
+TRAFFIC_PROFILE = {"laplace3d_cube_1M": "translate_symw_lap3d_1M.md"}  # per-launch DRAM bytes from ncu
 
 
 def run_single(args):
