@@ -169,6 +169,20 @@ int skf_skel_boxes(int32_t op, double kappa, int32_t nbox, const int64_t* off, c
                    void* stream);
 
 /*
+ * skf_skel_boxes over the boxes of one level of several trees at once (the
+ * builds of independent instances, one launch per level): box b's proxy
+ * surface has side 2.95 * box_lengths[b] (DEVICE, FP64 per box) about
+ * centers[b]; everything else as skf_skel_boxes (one operator, tolerance
+ * and proxy count for all boxes).  Replaces, like skf_skel_boxes, the
+ * reference's per-box skel_box_helper calls (skelfmm/util.py:381-437) of
+ * several RecursiveSkeletonization.skel_tree level loops.
+ */
+int skf_skel_boxes_multi(int32_t op, double kappa, int32_t nbox, const int64_t* off, const double* x,
+                         const double* geom, const double* centers, const double* box_lengths, int32_t nproxy,
+                         double tol, int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out,
+                         void* stream);
+
+/*
  * skf_skel_boxes without any device allocation.  No counterpart in the
  * reference: for callers that may not allocate GPU memory on this code path
  * (their own pool owns the device memory, a host framework's fixed budget, a

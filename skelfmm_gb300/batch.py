@@ -14,6 +14,8 @@ per-direction) and the packed kernel's block shape by timing them.
 
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -76,6 +78,80 @@ def concat_ragged(rbs):
     return out, np.asarray(starts, dtype=np.int64)
 
 
+def skel_trees_lockstep(fmms, npoints_max):
+    """``skel_tree(npoints_max)`` of every instance, level by level in step:
+    step k skeletonizes level nlevels_i - 1 - k of each instance i still
+    below its root, all of them (grouped by proxy count) in one
+    ``skf_skel_boxes_multi`` launch, each box with its own tree's proxy
+    surface.  The IDs are those of the per-instance level loop
+    (skelfmm/recursive_skel.py:370-498 per instance); only the launches are
+    shared.  Instances with a rank predictor are not supported."""
+    if not fmms:
+        return fmms
+    if any(f.rank_predictor is not None for f in fmms):
+        raise ValueError("the lockstep build runs the pivoted-QR IDs only")
+    f0 = fmms[0]
+    if any(f.op_id != f0.op_id or f.kappa != f0.kappa or f.tol != f0.tol or f.device != f0.device for f in fmms):
+        raise ValueError("instances must share the operator, kappa, tolerance and device")
+    dev = f0.device
+    lib = _lib.load()
+    tdt = torch.complex128 if is_complex_op(f0.op_id) else torch.float64
+    lev = {}
+    for i, f in enumerate(fmms):
+        f.root_level = max(0, f.tree.nlevels - 1)
+        if f.tree.nlevels - 1 >= 1:
+            lev[i] = f.tree.nlevels - 1
+    while lev:
+        groups = {}
+        for i in list(lev):
+            f, lv = fmms[i], lev[i]
+            if f._is_root_level(lv, npoints_max):
+                del lev[i]
+                continue
+            inp = f._level_inputs(lv)
+            groups.setdefault(inp["nproxy"], []).append((i, inp))
+        for nproxy, members in groups.items():
+            nb = [m[1]["nbl"] for m in members]
+            ne = [int(m[1]["off"][-1]) for m in members]
+            nt = [int(m[1]["cap"].sum()) for m in members]
+            b0 = np.concatenate(([0], np.cumsum(nb)))
+            e0 = np.concatenate(([0], np.cumsum(ne)))
+            t0 = np.concatenate(([0], np.cumsum(nt)))
+            off = np.concatenate([[0]] + [m[1]["off"][1:] + e0[k] for k, m in enumerate(members)]).astype(np.int64)
+            t_off = np.concatenate([m[1]["t_off"] + t0[k] for k, m in enumerate(members)]).astype(np.int64)
+            lens = np.concatenate([np.full(m[1]["nbl"], m[1]["length"]) for m in members])
+            centers = np.concatenate([m[1]["centers"] for m in members])
+            x = torch.cat([m[1]["x"] for m in members])
+            g = torch.cat([m[1]["g"] for m in members]) if members[0][1]["g"] is not None else None
+            t_buf = torch.zeros(max(int(t0[-1]), 1), dtype=tdt, device=dev)
+            rank = torch.zeros(int(b0[-1]), dtype=torch.int32, device=dev)
+            perm = torch.zeros(max(int(e0[-1]), 1), dtype=torch.int32, device=dev)
+            off_t = torch.from_numpy(off).to(dev)
+            t_off_t = torch.from_numpy(t_off).to(dev)
+            lens_t = torch.from_numpy(lens).to(dev)
+            cen_t = torch.from_numpy(np.ascontiguousarray(centers)).to(dev)
+            stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+            _lib.check(lib.skf_skel_boxes_multi(
+                f0.op_id, f0.kappa, int(b0[-1]), _lib.ptr(off_t), _lib.ptr(x), _lib.ptr(g), _lib.ptr(cen_t),
+                _lib.ptr(lens_t), int(nproxy), float(f0.tol), _lib.ptr(rank), _lib.ptr(perm), _lib.ptr(t_off_t),
+                _lib.ptr(t_buf), stream), "skf_skel_boxes_multi")
+            rank_h = rank.cpu().numpy()
+            perm_h = perm.cpu().numpy()
+            for k, (i, inp) in enumerate(members):
+                f = fmms[i]
+                f.level_stats[inp["lev"]] = {"boxes": inp["nbl"], "randomized": 0, "kept": 0, "fallback": 0,
+                                             "launch_boxes": int(b0[-1])}
+                f._level_finish(inp, rank_h[b0[k]:b0[k + 1]], perm_h[e0[k]:e0[k + 1]],
+                                t_buf[int(t0[k]):int(t0[k + 1])])
+                lev[i] -= 1
+                if lev[i] < 1:
+                    del lev[i]
+    _lib.check(lib.skf_trim_workspace(), "skf_trim_workspace")
+    for f in fmms:
+        f._entries_above_root()
+    return fmms
+
+
 def autotune(plan: Plan, precision=_lib.PREC_MIXED, reps=3):
     """Time the translation schemes this plan supports and keep the fastest
     (``Plan.autotune``).  Returns {setting: ms}."""
@@ -86,24 +162,30 @@ class SkelFMMBatch:
     """Independent instances (points_i, same operator) applied together.
 
     ``apply(xs)`` takes a list of charge vectors (or one concatenated vector)
-    and returns the list of potentials.  ``capture()`` records the device
+    and returns the list of potentials.  The instances' IDs run level by
+    level in step, one launch per level for all of them (``lockstep=False``:
+    one instance after another).  ``capture()`` records the device
     apply into a CUDA graph for the given precision; later applies replay it.
     """
 
     def __init__(self, point_sets, operator, tol=1e-6, leaf_size=128, param=0.0, geometries=None,
-                 npoints_max=500, precision="mixed", tune=True):
+                 npoints_max=500, precision="mixed", tune=True, lockstep=True):
         self.operator = operator
         self.param = param
         self.precision = precision
         self.point_sets = [np.asarray(p, dtype=np.float64) for p in point_sets]
         self.geometries = geometries
         self.sizes = [int(p.shape[0]) for p in point_sets]
+        fmms = [RecursiveSkeletonization(BalancedTree(pts, leaf_size, device="cuda"), operator, param, tol,
+                                         geometry=None if geometries is None else geometries[i])
+                for i, pts in enumerate(self.point_sets)]
+        if lockstep:
+            skel_trees_lockstep(fmms, npoints_max)
+        else:
+            for fmm in fmms:
+                fmm.skel_tree(npoints_max=npoints_max)
         rbs = []
-        for i, pts in enumerate(self.point_sets):
-            tree = BalancedTree(pts, leaf_size, device="cuda")
-            fmm = RecursiveSkeletonization(tree, operator, param, tol,
-                                           geometry=None if geometries is None else geometries[i])
-            fmm.skel_tree(npoints_max=npoints_max)
+        for fmm in fmms:
             fmm.setup_lists()
             rbs.append(fmm.ragged())
         self.instance_ragged = rbs

@@ -100,6 +100,7 @@ struct SkelArgs {
   int np;              // proxy points
   int mrows;           // rows of the proxy matrix (np or 2 np)
   double plen;         // proxy side = 2.95 * box length
+  const double* box_len;  // per-box side lengths (boxes of several trees), or NULL: plen for all
   double kappa;
   double tol;
   double* ws;          // column-major workspace
@@ -164,8 +165,8 @@ __device__ __forceinline__ double rsqrt_f64_1(double x) {
 // holds the box's proxy points (NULL: from the template).  FAST: 3D Laplace
 // entries from rsqrt_f64_1.
 template <int OP, bool FAST = false>
-__device__ __forceinline__ void proxy_entry(const SkelArgs& a, const double (&c)[3], const double* pts, int i,
-                                            const double* xj, const double* gj, double& kr, double& ki) {
+__device__ __forceinline__ void proxy_entry(const SkelArgs& a, const double (&c)[3], double plen, const double* pts,
+                                            int i, const double* xj, const double* gj, double& kr, double& ki) {
   constexpr int D = OpTraits<OP>::kDim;
   constexpr int G = OpTraits<OP>::kGeom;
   const int pi = (i < a.np) ? i : i - a.np;
@@ -173,7 +174,7 @@ __device__ __forceinline__ void proxy_entry(const SkelArgs& a, const double (&c)
   if (pts) {
     for (int d = 0; d < D; ++d) p[d] = pts[pi * D + d];
   } else {
-    for (int d = 0; d < D; ++d) p[d] = c[d] + a.plen * a.tmpl[pi * D + d];
+    for (int d = 0; d < D; ++d) p[d] = c[d] + plen * a.tmpl[pi * D + d];
   }
   if constexpr (FAST && OP == SKF_LAPLACE_3D) {
     const double dx = xj[0] - p[0], dy = xj[1] - p[1], dz = xj[2] - p[2];
@@ -663,7 +664,8 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
   double* A = a.ws + a.ws_off[lb];
   double c[3] = {0, 0, 0};
   for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
-  for (int i = threadIdx.x; i < a.np * D; i += blockDim.x) pts[i] = c[i % D] + a.plen * a.tmpl[i];
+  const double plen = a.box_len ? 2.95 * a.box_len[b] : a.plen;
+  for (int i = threadIdx.x; i < a.np * D; i += blockDim.x) pts[i] = c[i % D] + plen * a.tmpl[i];
   __syncthreads();
 
   // ---- 1. proxy matrix, column j = box point j (a warp per column)
@@ -680,7 +682,7 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
       if (gj) bad |= !(isfinite(gj[0]) && isfinite(gj[1]) && isfinite(gj[2]));
       for (int i = lane; i < m; i += 32) {
         double kr, ki;
-        proxy_entry<OP, RAND>(a, c, pts, i, xj, gj, kr, ki);
+        proxy_entry<OP, RAND>(a, c, plen, pts, i, xj, gj, kr, ki);
         col[i * W] = kr;
         if (C) col[i * W + 1] = ki;
         bad |= !isfinite(kr) || (C && !isfinite(ki));
@@ -1067,6 +1069,7 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double c[3] = {0, 0, 0};
   for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
+  const double plen = a.box_len ? 2.95 * a.box_len[b] : a.plen;
 
   // ---- proxy matrix, owned columns only (a warp per column)
   for (int jl = warp; jl < ncl; jl += nw) {
@@ -1079,7 +1082,7 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
     if (gj) bad |= !(isfinite(gj[0]) && isfinite(gj[1]) && isfinite(gj[2]));
     for (int i = lane; i < m; i += 32) {
       double kr, ki;
-      proxy_entry<OP>(a, c, nullptr, i, xj, gj, kr, ki);
+      proxy_entry<OP>(a, c, plen, nullptr, i, xj, gj, kr, ki);
       A[(int64_t)j * m + i] = kr;
       bad |= !isfinite(kr);
     }
@@ -1292,7 +1295,7 @@ int trim_workspace() {
 }
 
 static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
-                           const double* centers, double box_length, int nproxy, double tol,
+                           const double* centers, double box_length, const double* box_lens, int nproxy, double tol,
                            const RandomizedArgs& ra, int32_t* rank, int32_t* perm, const int64_t* t_off_out,
                            void* t_out, cudaStream_t st) {
   const int ndim = (op == SKF_LAPLACE_2D || op == SKF_HELMHOLTZ_2D) ? 2 : 3;
@@ -1420,6 +1423,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     a.np = np;
     a.mrows = mrows;
     a.plen = 2.95 * box_length;
+    a.box_len = box_lens;
     a.kappa = kappa;
     a.tol = tol;
     a.ws = ws;
@@ -1544,11 +1548,11 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
 }
 
 int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
-               const double* centers, double box_length, int nproxy, double tol, int32_t* rank, int32_t* perm,
-               const int64_t* t_off_out, void* t_out, cudaStream_t st) {
+               const double* centers, double box_length, const double* box_lens, int nproxy, double tol,
+               int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out, cudaStream_t st) {
   RandomizedArgs ra;
-  return skel_boxes_impl(op, kappa, nbox, off, x, geom, centers, box_length, nproxy, tol, ra, rank, perm, t_off_out,
-                         t_out, st);
+  return skel_boxes_impl(op, kappa, nbox, off, x, geom, centers, box_length, box_lens, nproxy, tol, ra, rank, perm,
+                         t_off_out, t_out, st);
 }
 
 int skel_boxes_randomized(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
@@ -1566,8 +1570,8 @@ int skel_boxes_randomized(int op, double kappa, int nbox, const int64_t* off, co
   ra.resid_tol = resid_tol;
   ra.resid = resid;
   ra.status = status;
-  return skel_boxes_impl(op, kappa, nbox, off, x, geom, centers, box_length, nproxy, tol, ra, rank, perm, t_off_out,
-                         t_out, st);
+  return skel_boxes_impl(op, kappa, nbox, off, x, geom, centers, box_length, nullptr, nproxy, tol, ra, rank, perm,
+                         t_off_out, t_out, st);
 }
 
 // Same work as skel_boxes, with the proxy template, the per-box workspace

@@ -23,8 +23,8 @@ int kernel_apply(int op, double kappa, int npairs, int mmax, int nmax, const int
                  const double* xt, const double* xs, const double* gt, const double* gs, const double* q,
                  const int8_t* sf, double* out, bool mixed, cudaStream_t st);
 int skel_boxes(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
-               const double* centers, double box_length, int nproxy, double tol, int32_t* rank, int32_t* perm,
-               const int64_t* t_off_out, void* t_out, cudaStream_t st);
+               const double* centers, double box_length, const double* box_lens, int nproxy, double tol,
+               int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out, cudaStream_t st);
 int skel_boxes_randomized(int op, double kappa, int nbox, const int64_t* off, const double* x, const double* geom,
                           const double* centers, double box_length, int nproxy, double tol, const int32_t* kpred,
                           int oversample, int rho, uint64_t seed, int nchk, double sketch_tol, double resid_tol,
@@ -643,8 +643,20 @@ int skf_skel_boxes(int32_t op, double kappa, int32_t nbox, const int64_t* off, c
   if (nbox == 0) return SKF_OK;
   if (!off || !x || !centers || !rank || !perm || !t_off_out || !t_out) return SKF_ERR_ARG;
   if (op_needs_geom(op) && !geom) return SKF_ERR_ARG;
-  return skel_boxes(op, kappa, nbox, off, x, geom, centers, box_length, nproxy, tol, rank, perm, t_off_out, t_out,
-                    static_cast<cudaStream_t>(stream));
+  return skel_boxes(op, kappa, nbox, off, x, geom, centers, box_length, nullptr, nproxy, tol, rank, perm, t_off_out,
+                    t_out, static_cast<cudaStream_t>(stream));
+}
+
+int skf_skel_boxes_multi(int32_t op, double kappa, int32_t nbox, const int64_t* off, const double* x,
+                         const double* geom, const double* centers, const double* box_lengths, int32_t nproxy,
+                         double tol, int32_t* rank, int32_t* perm, const int64_t* t_off_out, void* t_out,
+                         void* stream) {
+  if (op < 0 || op >= SKF_NUM_OPS || nbox < 0 || nproxy <= 0 || !(tol > 0)) return SKF_ERR_ARG;
+  if (nbox == 0) return SKF_OK;
+  if (!off || !x || !centers || !box_lengths || !rank || !perm || !t_off_out || !t_out) return SKF_ERR_ARG;
+  if (op_needs_geom(op) && !geom) return SKF_ERR_ARG;
+  return skel_boxes(op, kappa, nbox, off, x, geom, centers, 1.0, box_lengths, nproxy, tol, rank, perm, t_off_out,
+                    t_out, static_cast<cudaStream_t>(stream));
 }
 
 int skf_copy_segments(int64_t nseg, const int64_t* src_off, const int64_t* dst_off, const int64_t* len,

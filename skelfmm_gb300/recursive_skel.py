@@ -219,6 +219,27 @@ class RecursiveSkeletonization:
         """Entries of a level above the root: leaves hold their points."""
         self._level_candidates(lev)
 
+    def _level_inputs(self, lev):
+        """Device inputs of the IDs of every box at ``lev``: entry offsets,
+        gathered coordinates (and geometry), box centers, the T buffer and
+        its per-box offsets (capacity bs^2/4 + bs per box)."""
+        tree = self.tree
+        dev = self.device
+        ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+        off = self._off[lev]
+        bs = np.diff(off)
+        ids_t = torch.from_numpy(self._ids[lev]).to(dev)
+        x = self._XX_dev.index_select(0, ids_t).contiguous()
+        g = None
+        if self._geom_dev is not None:
+            g = self._geom_dev.index_select(0, ids_t).contiguous()
+        cap = (bs * bs) // 4 + bs
+        t_off = np.zeros(le - ls, dtype=np.int64)
+        np.cumsum(cap[:-1], out=t_off[1:])
+        return {"lev": lev, "nbl": le - ls, "off": off, "bs": bs, "x": x, "g": g,
+                "centers": np.ascontiguousarray(tree._box_center[ls:le]), "length": float(tree.L0 * 0.5 ** lev),
+                "nproxy": int(self.nproxy_level[lev]), "cap": cap, "t_off": t_off}
+
     def _skel_level(self, lev):
         """Proxy IDs of every box at ``lev`` on the GPU in one call.  With a
         rank predictor, every box whose predicted rank is below its size
@@ -229,29 +250,19 @@ class RecursiveSkeletonization:
         tree = self.tree
         dev = self.device
         ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
-        nbl = le - ls
-        off = self._off[lev]
-        bs = np.diff(off)
-        ids = self._ids[lev]
-        ids_t = torch.from_numpy(ids).to(dev)
-        x = self._XX_dev.index_select(0, ids_t).contiguous()
-        g = None
-        if self._geom_dev is not None:
-            g = self._geom_dev.index_select(0, ids_t).contiguous()
-        centers = torch.from_numpy(np.ascontiguousarray(tree._box_center[ls:le])).to(dev)
-        cplx = is_complex_op(self.op_id)
-        cap = (bs * bs) // 4 + bs
-        t_off = np.zeros(nbl, dtype=np.int64)
-        np.cumsum(cap[:-1], out=t_off[1:])
-        tdt = torch.complex128 if cplx else torch.float64
-        t_buf = torch.zeros(max(int(cap.sum()), 1), dtype=tdt, device=dev)
+        inp = self._level_inputs(lev)
+        nbl, off, bs, x, g = inp["nbl"], inp["off"], inp["bs"], inp["x"], inp["g"]
+        t_off = inp["t_off"]
+        centers = torch.from_numpy(inp["centers"]).to(dev)
+        tdt = torch.complex128 if is_complex_op(self.op_id) else torch.float64
+        t_buf = torch.zeros(max(int(inp["cap"].sum()), 1), dtype=tdt, device=dev)
         rank = torch.zeros(nbl, dtype=torch.int32, device=dev)
         perm = torch.zeros(max(int(off[-1]), 1), dtype=torch.int32, device=dev)
         off_t = torch.from_numpy(off).to(dev)
         t_off_t = torch.from_numpy(t_off).to(dev)
         stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
         lib = _lib.load()
-        length = float(tree.L0 * 0.5 ** lev)
+        length = inp["length"]
         mrows = self._mrows(lev)
         stats = {"boxes": nbl, "rows_full": int(mrows)}
         pred = None
@@ -288,9 +299,21 @@ class RecursiveSkeletonization:
                          sketch_rows=int(np.sum(np.where(st > 0, (kpred + self.oversample) * (2 ** rounds - 1), 0))))
             self._last_pred = pred
             self._last_status = st
-        rank_h = rank.cpu().numpy().astype(np.int64)
-        perm_h = perm.cpu().numpy().astype(np.int64)[: int(off[-1])]
         self.level_stats[lev] = stats
+        self._level_finish(inp, rank.cpu().numpy(), perm.cpu().numpy()[: int(off[-1])], t_buf)
+
+    def _level_finish(self, inp, rank_h, perm_h, t_buf):
+        """Skeleton-first entry order, ranks and compacted T blocks of level
+        ``inp["lev"]`` from the IDs' ranks, box-local pivot orders and the T
+        buffer (laid out at ``inp["t_off"]``)."""
+        lev, off, bs, t_off = inp["lev"], inp["off"], inp["bs"], inp["t_off"]
+        nbl = inp["nbl"]
+        ls, le = int(self.tree.level_sep[lev]), int(self.tree.level_sep[lev + 1])
+        dev = self.device
+        cplx = is_complex_op(self.op_id)
+        rank_h = np.asarray(rank_h).astype(np.int64)
+        perm_h = np.asarray(perm_h).astype(np.int64)
+        ids = self._ids[lev]
         # skeleton-first ids, candidate -> final position
         base = np.repeat(off[:-1], bs)
         src = base + perm_h
@@ -303,17 +326,18 @@ class RecursiveSkeletonization:
         tl = rank_h * (bs - rank_h)
         toff = np.zeros(nbl + 1, dtype=np.int64)
         np.cumsum(tl, out=toff[1:])
-        tc = torch.empty(max(int(toff[-1]), 1), dtype=tdt, device=dev)
+        tc = torch.empty(max(int(toff[-1]), 1), dtype=t_buf.dtype, device=dev)
         nz = np.flatnonzero(tl > 0)
         if nz.size:
             so = torch.from_numpy(t_off[nz]).to(dev)
             do = torch.from_numpy(toff[:-1][nz]).to(dev)
             ln = torch.from_numpy(tl[nz]).to(dev)
-            _lib.check(lib.skf_copy_segments(int(nz.size), _lib.ptr(so), _lib.ptr(do), _lib.ptr(ln), _lib.ptr(t_buf),
-                                             _lib.ptr(tc), 16 if cplx else 8, stream), "skf_copy_segments")
+            stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+            _lib.check(_lib.load().skf_copy_segments(int(nz.size), _lib.ptr(so), _lib.ptr(do), _lib.ptr(ln),
+                                                     _lib.ptr(t_buf), _lib.ptr(tc), 16 if cplx else 8, stream),
+                       "skf_copy_segments")
         self._tdev[lev] = tc
         self._toff[lev] = toff[:-1]
-        del t_buf
 
     def _mrows(self, lev):
         out = ctypes.c_int32()
@@ -329,14 +353,7 @@ class RecursiveSkeletonization:
         tree = self.tree
         self.root_level = max(0, tree.nlevels - 1)
         for lev in range(tree.nlevels - 1, 0, -1):
-            self._level_candidates(lev)
-            boxes_lev = tree.get_boxes_level(lev)
-            above = tree.get_leaves_above(lev)
-            npoints_lev = int(np.sum(self.bs_list[boxes_lev]) + np.sum(self.bs_list[above]))
-            if verbose:
-                print("\t Level %2d has %6d npoints" % (lev, npoints_lev))
-            if lev == 2 or npoints_lev <= npoints_max:
-                self.root_level = lev
+            if self._is_root_level(lev, npoints_max, verbose):
                 break
             t0 = perf_counter()
             self._skel_level(lev)
@@ -345,11 +362,29 @@ class RecursiveSkeletonization:
             if verbose:
                 print("\t Level %2d ids: %5.3f s" % (lev, self.level_times[lev]))
         _lib.check(_lib.load().skf_trim_workspace(), "skf_trim_workspace")
-        if tree.nlevels == 1:
+        self._entries_above_root()
+        return self
+
+    def _is_root_level(self, lev, npoints_max, verbose=False):
+        """Candidates of ``lev``; True (and ``root_level = lev``) when the
+        level loop stops there: level 2, or few enough points left
+        (recursive_skel.py:370-385)."""
+        tree = self.tree
+        self._level_candidates(lev)
+        npoints_lev = int(np.sum(self.bs_list[tree.get_boxes_level(lev)]) +
+                          np.sum(self.bs_list[tree.get_leaves_above(lev)]))
+        if verbose:
+            print("\t Level %2d has %6d npoints" % (lev, npoints_lev))
+        if lev == 2 or npoints_lev <= npoints_max:
+            self.root_level = lev
+            return True
+        return False
+
+    def _entries_above_root(self):
+        if self.tree.nlevels == 1:
             self._level_candidates(0)
         for lev in range(self.root_level - 1, -1, -1):
             self._leaf_level_entries(lev)
-        return self
 
     def setup_lists(self, verbose=False):
         """Translation lists (recursive_skel.py:622-712) and index maps

@@ -27,7 +27,8 @@ def test_batch_fp64_matches_single_instances(instances):
     from skelfmm_gb300.skel_fmm import SkelFMM
 
     pts, xs = instances
-    b = SkelFMMBatch(pts, operators.LAPLACE_2D, tol=1e-6, leaf_size=128, precision="fp64", tune=False)
+    b = SkelFMMBatch(pts, operators.LAPLACE_2D, tol=1e-6, leaf_size=128, precision="fp64", tune=False,
+                     lockstep=False)
     ys = b.apply(xs)
     for p, x, y in zip(pts, xs, ys):
         y1 = SkelFMM(p, operators.LAPLACE_2D, tol=1e-6, leaf_size=128).apply(x)
