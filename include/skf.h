@@ -57,6 +57,7 @@ extern "C" {
 #define SKF_KIND_ROOT 3        /* u += K q (dense root level)                       */
 
 typedef struct skf_plan skf_plan;
+typedef struct skf_tree skf_tree;
 
 /*
  * A built skeletonization in ragged (CSR) form.  "Entries" are the points a
@@ -295,6 +296,37 @@ int skf_box_moments(int32_t nbox, int32_t ndim, const int64_t* off, const double
  */
 int skf_morton_keys(int32_t ndim, int64_t n, const double* x, const double* corner, double L0, int32_t depth,
                     uint64_t* keys, int64_t* q, void* stream);
+
+/*
+ * Box levels and neighbour tables of the adaptive 2:1-balanced tree (the
+ * tree the reference takes from simpletree.BalancedTree, called at
+ * skelfmm/skel_fmm.py:150; its lists are read at
+ * skelfmm/recursive_skel.py:643-653, 692-699), on the device, from the
+ * point keys of skf_morton_keys sorted ascending (skeys: DEVICE [n]).
+ * A box with more than leaf_size points is split (up to level `depth`);
+ * then every leaf at level l-2 touching a box at level l is split until none
+ * is left.  Children that would be empty are not created.  Boxes are
+ * numbered level by level, in Morton order within a level.  *out receives a
+ * tree handle (device memory, released by skf_tree_destroy).
+ */
+int skf_tree_build(int32_t ndim, int64_t n, const uint64_t* skeys, int32_t depth, int64_t leaf_size,
+                   skf_tree** out, void* stream);
+int skf_tree_query(const skf_tree* tree, int32_t* nlevels, int64_t* nboxes);
+/*
+ * Copies the tree's arrays (host or device destinations, any may be NULL;
+ * returns after the copies are done): level_sep [nlevels + 1] (HOST) —
+ * boxes of level l are [level_sep[l], level_sep[l+1]); per box: code (the
+ * level's Morton code), coords [ndim] (integer cell at the box's level),
+ * start/end (range in the sorted point order), leaf (0/1), parent (-1 at the
+ * root), children [2^ndim] (Morton order, -1 padded), colleagues [3^ndim]
+ * (same-level boxes at offsets {-1,0,1}^ndim, axis 0 slowest, self
+ * included, -1 where absent) and coarse [2^ndim] (leaves one level up
+ * touching the box, parent excluded, compacted, -1 padded).
+ */
+int skf_tree_export(const skf_tree* tree, int64_t* level_sep, uint64_t* code, int64_t* coords, int64_t* start,
+                    int64_t* end, uint8_t* leaf, int64_t* parent, int64_t* children, int64_t* colleagues,
+                    int64_t* coarse, void* stream);
+void skf_tree_destroy(skf_tree* tree);
 
 const char* skf_status_string(int32_t status);
 int skf_version(void);

@@ -36,8 +36,9 @@ import itertools
 import numpy as np
 
 _MAX_DEPTH = {2: 30, 3: 20}
-# below this many points the host front end is faster than the device round trip
-DEVICE_FRONT_END_MIN_POINTS = 100_000
+# with a CUDA device given, clouds of at least this many points build their
+# tree there (faster from a few thousand points on; the trees are identical)
+DEVICE_FRONT_END_MIN_POINTS = 1
 
 
 def _spread_bits(v: np.ndarray, ndim: int, nbits: int) -> np.ndarray:
@@ -87,11 +88,12 @@ class BalancedTree:
     """Adaptive, 2:1-balanced tree over ``points[N, d]`` (d = 2 or 3)."""
 
     def __init__(self, points, leaf_size, device=None):
-        """``device``: a CUDA device (torch.device or string) to compute the
-        point-level front end there for clouds of DEVICE_FRONT_END_MIN_POINTS
-        or more (the points' integer cells and Morton keys in a CUDA kernel,
-        the stable key sort on the device); the box levels are then refined
-        on the host as without it, and the tree is identical."""
+        """``device``: a CUDA device (torch.device or string) to build the
+        tree there for clouds of DEVICE_FRONT_END_MIN_POINTS or more: the
+        points' integer cells and Morton keys in a CUDA kernel, the stable
+        key sort on the device, then the box levels, the 2:1 balance and the
+        neighbour tables from the sorted keys (skf_tree_build).  The tree is
+        identical to the host build."""
         XX = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
         if XX.ndim != 2 or XX.shape[1] not in (2, 3):
             raise ValueError("points must have shape (N, 2) or (N, 3)")
@@ -107,7 +109,10 @@ class BalancedTree:
         D = _MAX_DEPTH[ndim]
         self._depth = D
         if device is not None and str(device).startswith("cuda") and self.N >= DEVICE_FRONT_END_MIN_POINTS:
-            self._front_end_device(XX, device)
+            skeys = self._front_end_device(XX, device)
+            self._box_levels_device(skeys)
+            self._set_geometry()
+            return
         else:
             lo = XX.min(axis=0)
             hi = XX.max(axis=0)
@@ -162,7 +167,8 @@ class BalancedTree:
     def _front_end_device(self, XX, device):
         """Root box, integer cells, keys and the stable key order computed on
         ``device``: skf_morton_keys (the same FP64 steps as the host path)
-        and a stable device sort (ties keep the input order)."""
+        and a stable device sort (ties keep the input order).  Returns the
+        sorted keys (device)."""
         import torch
 
         from . import _lib
@@ -178,15 +184,72 @@ class BalancedTree:
         n, ndim = XX.shape
         ct = torch.from_numpy(np.ascontiguousarray(corner)).to(dev)
         keys = torch.empty(n, dtype=torch.int64, device=dev)
-        q = torch.empty((n, ndim), dtype=torch.int64, device=dev)
         _lib.check(_lib.load().skf_morton_keys(ndim, n, _lib.ptr(x), _lib.ptr(ct), float(self.L0), self._depth,
-                                                _lib.ptr(keys), _lib.ptr(q),
+                                                _lib.ptr(keys), None,
                                                 torch.cuda.current_stream(dev).cuda_stream), "skf_morton_keys")
         # keys < 2^63: the signed order is the unsigned one
         skeys, perm = torch.sort(keys, stable=True)
         self._perm = perm.cpu().numpy()
         self._skeys = skeys.cpu().numpy().view(np.uint64)
-        self._q = q.cpu().numpy()
+        return skeys
+
+    def _box_levels_device(self, skeys):
+        """Refinement, 2:1 balance and the neighbour tables on the device
+        (skf_tree_build over the sorted keys), copied into the host arrays
+        the host build fills."""
+        import ctypes
+
+        import torch
+
+        from . import _lib
+
+        lib = _lib.load()
+        ndim = self.ndim
+        h = ctypes.c_void_p()
+        stream = torch.cuda.current_stream(skeys.device).cuda_stream
+        _lib.check(lib.skf_tree_build(ndim, self.N, _lib.ptr(skeys), self._depth, self.leaf_size, ctypes.byref(h),
+                                      stream), "skf_tree_build")
+        try:
+            nlev, nb = ctypes.c_int32(), ctypes.c_int64()
+            _lib.check(lib.skf_tree_query(h, ctypes.byref(nlev), ctypes.byref(nb)), "skf_tree_query")
+            nlev, nb = int(nlev.value), int(nb.value)
+            nc, nq = 1 << ndim, 3 ** ndim
+            level_sep = np.zeros(nlev + 1, dtype=np.int64)
+            code = np.empty(nb, dtype=np.uint64)
+            coords = np.empty((nb, ndim), dtype=np.int64)
+            start = np.empty(nb, dtype=np.int64)
+            end = np.empty(nb, dtype=np.int64)
+            leaf = np.empty(nb, dtype=np.uint8)
+            parent = np.empty(nb, dtype=np.int64)
+            children = np.empty((nb, nc), dtype=np.int64)
+            colleagues = np.empty((nb, nq), dtype=np.int64)
+            coarse = np.empty((nb, nc), dtype=np.int64)
+            _lib.check(lib.skf_tree_export(h, *(_lib.ptr(a) for a in (
+                level_sep, code, coords, start, end, leaf, parent, children, colleagues, coarse)), stream),
+                "skf_tree_export")
+        finally:
+            lib.skf_tree_destroy(h)
+        leaf = leaf.astype(bool)
+        sl = [slice(int(level_sep[l]), int(level_sep[l + 1])) for l in range(nlev)]
+        self._Lc = [coords[s] for s in sl]
+        self._Lk = [code[s] for s in sl]
+        self._Ls = [start[s] for s in sl]
+        self._Le = [end[s] for s in sl]
+        self._Lleaf = [leaf[s] for s in sl]
+        self.nlevels = nlev
+        self.level_sep = level_sep
+        self.nboxes = nb
+        self._box_coords = coords
+        self._box_start = start
+        self._box_end = end
+        self._is_leaf = leaf
+        self._box_level = np.repeat(np.arange(nlev, dtype=np.int64), np.diff(level_sep))
+        self._leaves = np.flatnonzero(leaf).astype(np.int64)
+        self.nleaves = int(self._leaves.shape[0])
+        self._children = children
+        self._parent = parent
+        self._colleagues = colleagues
+        self._coarse = coarse
 
     def _lookup(self, lev, coords):
         """Index within level ``lev`` of the boxes at integer ``coords``, -1 if absent."""
@@ -341,7 +404,9 @@ class BalancedTree:
             coarse[base:base + n] = np.take_along_axis(found, order, axis=1)
         self._colleagues = colleagues
         self._coarse = coarse
+        self._set_geometry()
 
+    def _set_geometry(self):
         lengths = self.L0 * np.power(0.5, self._box_level.astype(np.float64))
         corner = self.c0 - 0.5 * self.L0
         self._box_length = lengths

@@ -1,7 +1,10 @@
-"""The tree's device front end (skf_morton_keys and a stable device sort)
-against the host build: every level array, the point order and the
-neighbour tables are identical, on the golden point sets and on 4e6 points
-in 32 Gaussian clusters (the learned-rank workload)."""
+"""The device tree (skf_morton_keys, a stable device sort, then
+skf_tree_build: refinement, 2:1 balance and neighbour tables from the sorted
+keys) against the host build: every level array, the point order and the
+neighbour tables are identical, on the golden point sets, on degenerate sets
+(coincident points down to the finest level, points on a line, a single
+point) and on 4e6 points in 32 Gaussian clusters (the learned-rank
+workload)."""
 import time
 
 import numpy as np
@@ -20,8 +23,21 @@ def _same(a, b):
     for name in ("_Lc", "_Lk", "_Ls", "_Le", "_Lleaf"):
         for la, lb in zip(getattr(a, name), getattr(b, name)):
             assert np.array_equal(la, lb), name
-    for name in ("_children", "_parent", "_colleagues", "_coarse", "_box_center", "_box_length", "_leaves"):
+    for name in ("_children", "_parent", "_colleagues", "_coarse", "_box_center", "_box_length", "_leaves",
+                 "level_sep", "_box_coords", "_box_start", "_box_end", "_is_leaf", "_box_level"):
         assert np.array_equal(getattr(a, name), getattr(b, name)), name
+        assert getattr(a, name).dtype == getattr(b, name).dtype, name
+
+
+def _device_tree(points, leaf):
+    from skelfmm_gb300 import tree as T
+
+    saved = T.DEVICE_FRONT_END_MIN_POINTS
+    T.DEVICE_FRONT_END_MIN_POINTS = 1
+    try:
+        return T.BalancedTree(points, leaf, device="cuda")
+    finally:
+        T.DEVICE_FRONT_END_MIN_POINTS = saved
 
 
 @pytest.mark.parametrize("name", build_cases())
@@ -31,13 +47,37 @@ def test_device_front_end_gives_the_host_tree_on_golden_points(name):
     from skelfmm_gb300 import tree as T
 
     d = load_build(name)
-    saved = T.DEVICE_FRONT_END_MIN_POINTS
-    T.DEVICE_FRONT_END_MIN_POINTS = 1  # the golden sets are smaller than the threshold
-    try:
-        b = BalancedTree(d["points"], int(d["leaf_size"]), device="cuda")
-    finally:
-        T.DEVICE_FRONT_END_MIN_POINTS = saved
+    # (the golden sets are smaller than the device threshold)
+    b = _device_tree(d["points"], int(d["leaf_size"]))
     _same(BalancedTree(d["points"], int(d["leaf_size"])), b)
+
+
+def _degenerate_sets():
+    rng = np.random.default_rng(11)
+    out = []
+    for ndim in (2, 3):
+        p = rng.random((3000, ndim))
+        p[100:400] = p[7]  # 300 coincident points: split down to the finest level
+        out.append((f"coincident_{ndim}d", p, 16))
+        t = rng.random(5000)
+        line = np.stack([t] + [t * 1e-9] * (ndim - 1), axis=1)
+        out.append((f"line_{ndim}d", line, 8))
+        out.append((f"single_{ndim}d", rng.random((1, ndim)), 4))
+        g = np.concatenate((rng.random((2000, ndim)) * 1e-4, rng.random((2000, ndim))))
+        out.append((f"dense_corner_{ndim}d", g, 10))
+    return out
+
+
+@pytest.mark.parametrize("case", _degenerate_sets(), ids=lambda c: c[0])
+def test_device_tree_on_degenerate_sets(case):
+    from skelfmm_gb300.tree import BalancedTree
+
+    _, pts, leaf = case
+    a = BalancedTree(pts, leaf)
+    b = _device_tree(pts, leaf)
+    _same(a, b)
+    if pts.shape[0] > 1 and "coincident" in case[0]:
+        assert a.nlevels == a._depth + 1
 
 
 def test_device_front_end_on_4e6_clustered_points():
