@@ -328,6 +328,28 @@ int skf_tree_export(const skf_tree* tree, int64_t* level_sep, uint64_t* code, in
                     int64_t* coarse, void* stream);
 void skf_tree_destroy(skf_tree* tree);
 
+/*
+ * Translation lists of a skeletonized tree on the device, grouped by target
+ * box (replaces the list construction of skelfmm/recursive_skel.py:622-712,
+ * get_parallel_lists): for a box b below root_level, its colleagues (row
+ * order, KIND_COLLEAGUE) then its coarse neighbours (row order,
+ * KIND_COARSE_UP); for every box s, the boxes below root_level that list s
+ * as a coarse neighbour, ascending (KIND_COARSE_DOWN); for a root box (in
+ * root_boxes: leaves above root_level and the boxes at it, ascending),
+ * every root box (KIND_ROOT).  Tables as skf_tree_export writes them
+ * (colleagues [nb x 3^ndim], coarse and children [nb x 2^ndim], int64);
+ * box_level [nb] int64.  All arrays DEVICE.  skf_lists_count writes
+ * list_off [nb + 1] (DEVICE) and the list length to *total (HOST; returns
+ * after the stream is done); skf_lists_fill writes list_src (int32) and
+ * list_kind (int8) at those offsets.
+ */
+int skf_lists_count(int32_t ndim, int64_t nboxes, const int64_t* colleagues, const int64_t* coarse,
+                    const int64_t* children, const int64_t* box_level, int32_t root_level, const int64_t* root_boxes,
+                    int64_t nroot, int64_t* list_off, int64_t* total, void* stream);
+int skf_lists_fill(int32_t ndim, int64_t nboxes, const int64_t* colleagues, const int64_t* coarse,
+                   const int64_t* children, const int64_t* box_level, int32_t root_level, const int64_t* root_boxes,
+                   int64_t nroot, const int64_t* list_off, int32_t* list_src, int8_t* list_kind, void* stream);
+
 const char* skf_status_string(int32_t status);
 int skf_version(void);
 

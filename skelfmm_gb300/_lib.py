@@ -82,6 +82,8 @@ SIGNATURES = {
     "skf_tree_query": (_i32, [_p, _p, _p]),
     "skf_tree_export": (_i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     "skf_tree_destroy": (None, [_p]),
+    "skf_lists_count": (_i32, [_i32, _i64, _p, _p, _p, _p, _i32, _p, _i64, _p, _p, _p]),
+    "skf_lists_fill": (_i32, [_i32, _i64, _p, _p, _p, _p, _i32, _p, _i64, _p, _p, _p, _p]),
     "skf_skel_boxes_multi": (_i32, [_i32, _f64, _i32, _p, _p, _p, _p, _p, _i32, _f64, _p, _p, _p, _p, _p]),
     "skf_trim_workspace": (_i32, []),
     "skf_mlp_num_params": (_i64, [_i32]),

@@ -525,3 +525,180 @@ extern "C" int skf_tree_export(const skf_tree* t, int64_t* level_sep, uint64_t* 
 }
 
 extern "C" void skf_tree_destroy(skf_tree* t) { delete t; }
+
+// ---------------------------------------------------------------------------
+// Translation lists on the device (the lists of
+// skelfmm/recursive_skel.py:622-712, grouped by target box): for a target
+// box b below the root level, its colleagues (row order, self included,
+// KIND_COLLEAGUE) and its coarse neighbours (row order, KIND_COARSE_UP);
+// for every box s, the boxes t below the root level that list s as a
+// coarse neighbour, ascending (KIND_COARSE_DOWN); for a root box (a leaf
+// above the root level or a box at it), every root box ascending
+// (KIND_ROOT).  A box t listing s as a coarse neighbour is a child of a
+// colleague of s other than s, so the down list is found from s's
+// colleagues (sorted) and their children (consecutive, ascending).
+// ---------------------------------------------------------------------------
+
+namespace skf {
+namespace tree {
+
+struct ListArgs {
+  int64_t nb = 0;
+  int nq = 0, nc = 0;
+  const int64_t* colleagues = nullptr;
+  const int64_t* coarse = nullptr;
+  const int64_t* children = nullptr;
+  const int64_t* level = nullptr;
+  int64_t root_level = 0;
+  const int64_t* root_boxes = nullptr;
+  int64_t nroot = 0;
+};
+
+__device__ __forceinline__ bool lists_as_coarse(const ListArgs& a, int64_t t, int64_t s) {
+  for (int k = 0; k < a.nc; ++k) {
+    const int64_t v = a.coarse[t * a.nc + k];
+    if (v < 0) break;
+    if (v == s) return true;
+  }
+  return false;
+}
+
+// Visits the coarse-down sources of box s in ascending order.
+template <class F>
+__device__ __forceinline__ void for_down(const ListArgs& a, int64_t s, F&& f) {
+  int64_t col[27];
+  int m = 0;
+  for (int k = 0; k < a.nq; ++k) {
+    const int64_t p = a.colleagues[s * a.nq + k];
+    if (p < 0 || p == s) continue;
+    int j = m++;
+    while (j > 0 && col[j - 1] > p) {
+      col[j] = col[j - 1];
+      --j;
+    }
+    col[j] = p;
+  }
+  for (int i = 0; i < m; ++i)
+    for (int c = 0; c < a.nc; ++c) {
+      const int64_t t = a.children[col[i] * a.nc + c];
+      if (t < 0) break;
+      if (a.level[t] > a.root_level && lists_as_coarse(a, t, s)) f(t);
+    }
+}
+
+__device__ __forceinline__ bool is_root_box(const ListArgs& a, int64_t b) {
+  int64_t lo = 0, hi = a.nroot;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (a.root_boxes[mid] < b)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo < a.nroot && a.root_boxes[lo] == b;
+}
+
+__global__ void k_list_count(ListArgs a, int64_t* cnt) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nb) return;
+  int64_t c = 0;
+  if (a.level[b] > a.root_level) {
+    for (int k = 0; k < a.nq; ++k) c += a.colleagues[b * a.nq + k] >= 0;
+    for (int k = 0; k < a.nc; ++k) c += a.coarse[b * a.nc + k] >= 0;
+  }
+  for_down(a, b, [&](int64_t) { ++c; });
+  if (is_root_box(a, b)) c += a.nroot;
+  cnt[b] = c;
+}
+
+__global__ void k_list_fill(ListArgs a, const int64_t* off, int32_t* src, int8_t* kind) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nb) return;
+  int64_t o = off[b];
+  if (a.level[b] > a.root_level) {
+    for (int k = 0; k < a.nq; ++k) {
+      const int64_t v = a.colleagues[b * a.nq + k];
+      if (v < 0) continue;
+      src[o] = (int32_t)v;
+      kind[o++] = SKF_KIND_COLLEAGUE;
+    }
+    for (int k = 0; k < a.nc; ++k) {
+      const int64_t v = a.coarse[b * a.nc + k];
+      if (v < 0) continue;
+      src[o] = (int32_t)v;
+      kind[o++] = SKF_KIND_COARSE_UP;
+    }
+  }
+  for_down(a, b, [&](int64_t t) {
+    src[o] = (int32_t)t;
+    kind[o++] = SKF_KIND_COARSE_DOWN;
+  });
+  if (is_root_box(a, b))
+    for (int64_t r = 0; r < a.nroot; ++r) {
+      src[o] = (int32_t)a.root_boxes[r];
+      kind[o++] = SKF_KIND_ROOT;
+    }
+}
+
+}  // namespace tree
+}  // namespace skf
+
+namespace {
+
+int list_args(int32_t ndim, int64_t nboxes, const int64_t* colleagues, const int64_t* coarse, const int64_t* children,
+              const int64_t* box_level, int32_t root_level, const int64_t* root_boxes, int64_t nroot,
+              skf::tree::ListArgs& a) {
+  if ((ndim != 2 && ndim != 3) || nboxes < 1 || nboxes > INT32_MAX || nroot < 0 || nroot > nboxes ||
+      root_level < 0 || !colleagues || !coarse || !children || !box_level || (nroot > 0 && !root_boxes))
+    return SKF_ERR_ARG;
+  a.nb = nboxes;
+  a.nq = ndim == 2 ? 9 : 27;
+  a.nc = 1 << ndim;
+  a.colleagues = colleagues;
+  a.coarse = coarse;
+  a.children = children;
+  a.level = box_level;
+  a.root_level = root_level;
+  a.root_boxes = root_boxes;
+  a.nroot = nroot;
+  return SKF_OK;
+}
+
+}  // namespace
+
+extern "C" int skf_lists_count(int32_t ndim, int64_t nboxes, const int64_t* colleagues, const int64_t* coarse,
+                               const int64_t* children, const int64_t* box_level, int32_t root_level,
+                               const int64_t* root_boxes, int64_t nroot, int64_t* list_off, int64_t* total,
+                               void* stream) {
+  using namespace skf::tree;
+  ListArgs a;
+  const int s = list_args(ndim, nboxes, colleagues, coarse, children, box_level, root_level, root_boxes, nroot, a);
+  if (s != SKF_OK) return s;
+  if (!list_off || !total) return SKF_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int64_t* cnt = nullptr;
+  SKF_CUDA_TRY(cudaMallocAsync(&cnt, sizeof(int64_t) * nboxes, st));
+  k_list_count<<<nblk(nboxes), kTB, 0, st>>>(a, cnt);
+  k_scan<<<1, 1024, 0, st>>>(nboxes, cnt, list_off);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(total, list_off + nboxes, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(cnt, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  SKF_CUDA_TRY(e);
+  return SKF_OK;
+}
+
+extern "C" int skf_lists_fill(int32_t ndim, int64_t nboxes, const int64_t* colleagues, const int64_t* coarse,
+                              const int64_t* children, const int64_t* box_level, int32_t root_level,
+                              const int64_t* root_boxes, int64_t nroot, const int64_t* list_off, int32_t* list_src,
+                              int8_t* list_kind, void* stream) {
+  using namespace skf::tree;
+  ListArgs a;
+  const int s = list_args(ndim, nboxes, colleagues, coarse, children, box_level, root_level, root_boxes, nroot, a);
+  if (s != SKF_OK) return s;
+  if (!list_off || !list_src || !list_kind) return SKF_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  k_list_fill<<<nblk(nboxes), kTB, 0, st>>>(a, list_off, list_src, list_kind);
+  SKF_CUDA_TRY(cudaGetLastError());
+  return SKF_OK;
+}

@@ -386,14 +386,11 @@ class RecursiveSkeletonization:
         for lev in range(self.root_level - 1, -1, -1):
             self._leaf_level_entries(lev)
 
-    def setup_lists(self, verbose=False):
-        """Translation lists (recursive_skel.py:622-712) and index maps
-        (recursive_skel.py:714-780), built directly in ragged form."""
+    def _lists_host(self):
+        """The translation lists in CSR by target box, with numpy (the same
+        lists as ``_lists_device``)."""
         tree = self.tree
-        nb = self.nboxes
-        levels = tree.get_boxes_levels()
-        leaf_mask = tree._is_leaf
-        below = levels > self.root_level
+        below = tree.get_boxes_levels() > self.root_level
         boxes_below = np.flatnonzero(below)
         col = tree.get_boxes_colleague_neigh_fullvec(boxes_below)
         t = np.repeat(boxes_below, col.shape[1])
@@ -403,17 +400,49 @@ class RecursiveSkeletonization:
         t = np.repeat(boxes_below, crs.shape[1])
         s = crs.ravel()
         up = np.stack((t[s >= 0], s[s >= 0]), 1)
-        root_boxes = np.hstack((tree.get_leaves_above(self.root_level),
-                                tree.get_boxes_level(self.root_level))).astype(np.int64)
-        root = np.stack((np.repeat(root_boxes, root_boxes.shape[0]),
-                         np.tile(root_boxes, root_boxes.shape[0])), 1)
-        self.root_boxes = root_boxes
-        self.skel_leaves = np.setdiff1d(tree.get_leaves(), tree.get_leaves_above(self.root_level + 1))
-        self.colleague_pairs = coll
-        self.coarse_up_pairs = up
-        self.list_off, self.list_src, self.list_kind = lists_to_csr(nb, [
+        rb = self.root_boxes
+        root = np.stack((np.repeat(rb, rb.shape[0]), np.tile(rb, rb.shape[0])), 1)
+        return lists_to_csr(self.nboxes, [
             (_lib.KIND_COLLEAGUE, coll), (_lib.KIND_COARSE_UP, up),
             (_lib.KIND_COARSE_DOWN, up[:, ::-1]), (_lib.KIND_ROOT, root)])
+
+    def _lists_device(self):
+        """The translation lists in CSR by target box, built on the device
+        from the tree's neighbour tables (skf_lists_count / skf_lists_fill)."""
+        tree = self.tree
+        dev = self.device
+        lib = _lib.load()
+
+        def up(a):
+            return torch.from_numpy(np.ascontiguousarray(a, dtype=np.int64)).to(dev)
+
+        col, crs, ch, lev = up(tree._colleagues), up(tree._coarse), up(tree._children), up(tree._box_level)
+        rb = up(self.root_boxes)
+        nb = self.nboxes
+        off = torch.empty(nb + 1, dtype=torch.int64, device=dev)
+        total = ctypes.c_int64()
+        stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        args = (self.ndim, nb, _lib.ptr(col), _lib.ptr(crs), _lib.ptr(ch), _lib.ptr(lev), int(self.root_level),
+                _lib.ptr(rb), int(rb.shape[0]))
+        _lib.check(lib.skf_lists_count(*args, _lib.ptr(off), ctypes.byref(total), stream), "skf_lists_count")
+        n = int(total.value)
+        src = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        kind = torch.empty(max(n, 1), dtype=torch.int8, device=dev)
+        _lib.check(lib.skf_lists_fill(*args, _lib.ptr(off), _lib.ptr(src), _lib.ptr(kind), stream), "skf_lists_fill")
+        return off.cpu().numpy(), src[:n].cpu().numpy(), kind[:n].cpu().numpy()
+
+    def setup_lists(self, verbose=False):
+        """Translation lists (recursive_skel.py:622-712, on the device) and
+        index maps (recursive_skel.py:714-780), built directly in ragged
+        form."""
+        tree = self.tree
+        nb = self.nboxes
+        leaf_mask = tree._is_leaf
+        root_boxes = np.hstack((tree.get_leaves_above(self.root_level),
+                                tree.get_boxes_level(self.root_level))).astype(np.int64)
+        self.root_boxes = root_boxes
+        self.skel_leaves = np.setdiff1d(tree.get_leaves(), tree.get_leaves_above(self.root_level + 1))
+        self.list_off, self.list_src, self.list_kind = self._lists_device()
 
         # entries: levels in order, boxes in order (levels above the root:
         # leaves only)

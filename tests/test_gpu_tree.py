@@ -94,3 +94,37 @@ def test_device_front_end_on_4e6_clustered_points():
     t2 = time.perf_counter()
     _same(a, b)
     print(f"host tree {t1 - t0:.3f} s, device front end {t2 - t1:.3f} s")
+
+
+def _lists_cases():
+    out = [(n, None) for n in build_cases()]
+    out += [(c[0], c) for c in _degenerate_sets() if not c[0].startswith("single")]
+    return out
+
+
+@pytest.mark.parametrize("case", _lists_cases(), ids=lambda c: c[0])
+def test_device_lists_equal_host_lists_at_every_root_level(case):
+    """skf_lists_count / skf_lists_fill against the numpy lists on the same
+    tree, for every possible root level."""
+    import torch
+
+    from skelfmm_gb300.recursive_skel import RecursiveSkeletonization
+
+    name, deg = case
+    if deg is None:
+        d = load_build(name)
+        pts, leaf = d["points"], int(d["leaf_size"])
+    else:
+        _, pts, leaf = deg
+    tree = _device_tree(pts, leaf)
+    # only the tree and the root level enter the lists (no skeletonization,
+    # so leaves of coincident points above leaf_size are allowed here)
+    fmm = RecursiveSkeletonization.__new__(RecursiveSkeletonization)
+    fmm.tree, fmm.nboxes, fmm.ndim, fmm.device = tree, tree.nboxes, tree.ndim, torch.device("cuda")
+    for root in range(tree.nlevels):
+        fmm.root_level = root
+        fmm.root_boxes = np.hstack((tree.get_leaves_above(root), tree.get_boxes_level(root))).astype(np.int64)
+        h = fmm._lists_host()
+        g = fmm._lists_device()
+        for a, b in zip(h, g):
+            assert a.dtype == b.dtype and np.array_equal(a, b), (name, root)
