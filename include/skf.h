@@ -92,6 +92,8 @@ typedef struct {
   const int8_t* list_kind;     /* [L] SKF_KIND_* */
   int32_t t_on_device;         /* 1: t_data is a DEVICE pointer (copied device to
                                   device), 0: host pointer like the rest */
+  int32_t entries_on_device;   /* 1: entry_xyz and entry_geom are DEVICE pointers,
+                                  0: host pointers like the rest */
 } skf_plan_desc;
 
 typedef struct {

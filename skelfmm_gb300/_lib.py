@@ -47,6 +47,7 @@ class PlanDesc(ctypes.Structure):
         ("nperm", _i64), ("perm_entry", _p), ("perm_point", _p),
         ("t_off", _p), ("t_data", _p), ("t_len", _i64),
         ("list_off", _p), ("list_src", _p), ("list_kind", _p), ("t_on_device", _i32),
+        ("entries_on_device", _i32),
     ]
 
 

@@ -62,19 +62,23 @@ def concat_ragged(rbs):
         toff += int(rb.t_data.shape[0])
         loff += int(rb.list_off[-1])
         starts.append(poff)
+    def cat(parts):
+        # device parts stay on the device
+        if not any(isinstance(a, torch.Tensor) for a in parts):
+            return np.concatenate(parts)
+        dev = next(a.device for a in parts if isinstance(a, torch.Tensor))
+        return torch.cat([a if isinstance(a, torch.Tensor) else torch.from_numpy(np.asarray(a)).to(dev)
+                          for a in parts])
+
     out = RaggedBuild(
         op=op, ndim=rbs[0].ndim, kappa=rbs[0].kappa, npoints=int(poff), nlevels=int(nlev), root_level=int(R),
         box_level=np.concatenate(box_level), box_off=np.concatenate(box_off), box_rank=np.concatenate(box_rank),
-        entry_xyz=np.concatenate(xyz), entry_geom=np.concatenate(geom) if geom else None,
+        entry_xyz=cat(xyz), entry_geom=cat(geom) if geom else None,
         entry_pslot=np.concatenate(pslot), perm_entry=np.concatenate(pe), perm_point=np.concatenate(pp),
         t_off=np.concatenate(t_off), t_data=None, list_off=np.concatenate(list_off),
         list_src=np.concatenate(list_src).astype(np.int32), list_kind=np.concatenate(list_kind),
     )
-    if not any(isinstance(t, torch.Tensor) for t in t_data):
-        out.t_data = np.concatenate(t_data)
-    else:
-        dev = next(t.device for t in t_data if isinstance(t, torch.Tensor))
-        out.t_data = torch.cat([t if isinstance(t, torch.Tensor) else torch.from_numpy(t).to(dev) for t in t_data])
+    out.t_data = cat(t_data)
     return out, np.asarray(starts, dtype=np.int64)
 
 

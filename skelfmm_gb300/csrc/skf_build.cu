@@ -159,6 +159,57 @@ __device__ __forceinline__ double rsqrt_f64_1(double x) {
   return fma(0.5 * y, e, y);
 }
 
+// 3D Laplace proxy-matrix entries on the FP32 pipes (GB300 issues FP64 at
+// 1/64 of the FP32 rate): 1/|x - p| as an unevaluated FP32 pair hi + lo with
+// relative error ~1e-13, from u = x - c and v = p - c (c the box centre)
+// held as FP32 pairs.  d = u - v by TwoSum (Knuth) plus the low parts; r^2
+// from exact squares (FMA residuals) and TwoSums; 1/r from the hardware
+// estimate y0 and one Newton step in pair arithmetic, y = y0 + y0 (1 -
+// r^2 y0^2) / 2, where 1 - fl(r^2 y0^2) is exact (Sterbenz).  Used for the
+// matrices that feed a sketch and its residual check (randomized IDs).
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ float2 lap3d_pair(const float (&uh)[3], const float (&ul)[3], const float* vh,
+                                             const float* vl) {
+  float dh[3], dl[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    two_sum_f(uh[k], -vh[k], dh[k], dl[k]);
+    dl[k] = __fadd_rn(dl[k], __fsub_rn(ul[k], vl[k]));
+  }
+  // r^2 = sum dh^2 + 2 dh dl (dl^2 below the pair's precision)
+  float p[3], pe[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    p[k] = __fmul_rn(dh[k], dh[k]);
+    pe[k] = __fmaf_rn(dh[k], dh[k], -p[k]);
+  }
+  float h, e1, e2;
+  two_sum_f(p[0], p[1], h, e1);
+  two_sum_f(h, p[2], h, e2);
+  float l = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fadd_rn(pe[0], pe[1]), pe[2]));
+  l = __fmaf_rn(__fmul_rn(2.f, dh[0]), dl[0], l);
+  l = __fmaf_rn(__fmul_rn(2.f, dh[1]), dl[1], l);
+  l = __fmaf_rn(__fmul_rn(2.f, dh[2]), dl[2], l);
+  const float H = __fadd_rn(h, l);
+  const float L = __fsub_rn(l, __fsub_rn(H, h));
+  // 1/r: y0 ~ 1/sqrt(H), then one Newton step with t = r^2 y0^2 in pairs
+  const float y0 = rsqrtf(H);
+  const float a = __fmul_rn(y0, y0);
+  const float b = __fmaf_rn(y0, y0, -a);
+  const float t = __fmul_rn(H, a);
+  const float te = __fmaf_rn(H, a, -t);
+  const float rest = __fmaf_rn(L, a, __fmaf_rn(H, b, te));
+  const float delta = __fsub_rn(__fsub_rn(1.f, t), rest);
+  return make_float2(y0, __fmul_rn(__fmul_rn(0.5f, y0), delta));
+}
+
+__device__ __forceinline__ double pair_to_f64(float2 v) { return __dadd_rn((double)v.x, (double)v.y); }
+
 // Entry (row i, box point x) of the stacked proxy matrix: rows [0, np) are
 // K(x, p_i) (target = box point), rows [np, 2 np) of the geometry operators
 // K(p_i, x) (target = proxy).  Sphere proxies carry radial normals.  `pts`
@@ -665,7 +716,21 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
   double c[3] = {0, 0, 0};
   for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
   const double plen = a.box_len ? 2.95 * a.box_len[b] : a.plen;
-  for (int i = threadIdx.x; i < a.np * D; i += blockDim.x) pts[i] = c[i % D] + plen * a.tmpl[i];
+  // 3D Laplace boxes of a randomized launch keep K as FP32 pairs (lap3d_pair)
+  // in the FP64 slots: it only feeds the sketch and the residual check
+  const bool pairs = RAND && OP == SKF_LAPLACE_3D && sketch && m == a.np;
+  float* vh = reinterpret_cast<float*>(pts);  // pairs: p_i - c as FP32 pairs
+  float* vl = vh + a.np * 3;
+  if (pairs) {
+    for (int i = threadIdx.x; i < a.np * 3; i += blockDim.x) {
+      const double v = plen * a.tmpl[i];
+      const float h = __double2float_rn(v);
+      vh[i] = h;
+      vl[i] = __double2float_rn(v - (double)h);
+    }
+  } else {
+    for (int i = threadIdx.x; i < a.np * D; i += blockDim.x) pts[i] = c[i % D] + plen * a.tmpl[i];
+  }
   __syncthreads();
 
   // ---- 1. proxy matrix, column j = box point j (a warp per column)
@@ -680,17 +745,37 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
       bool bad = false;
       for (int d = 0; d < D; ++d) bad |= !isfinite(xj[d]);
       if (gj) bad |= !(isfinite(gj[0]) && isfinite(gj[1]) && isfinite(gj[2]));
-      for (int i = lane; i < m; i += 32) {
-        double kr, ki;
-        proxy_entry<OP, RAND>(a, c, plen, pts, i, xj, gj, kr, ki);
-        col[i * W] = kr;
-        if (C) col[i * W + 1] = ki;
-        bad |= !isfinite(kr) || (C && !isfinite(ki));
+      if (pairs) {
+        float uh[3], ul[3];
+        for (int d = 0; d < 3; ++d) {
+          const double u = xj[d] - c[d];
+          uh[d] = __double2float_rn(u);
+          ul[d] = __double2float_rn(u - (double)uh[d]);
+        }
+        float2* colp = reinterpret_cast<float2*>(col);
+        for (int i = lane; i < m; i += 32) {
+          const float2 k = lap3d_pair(uh, ul, vh + 3 * i, vl + 3 * i);
+          colp[i] = k;
+          bad |= !isfinite(k.x);
+        }
+      } else {
+        for (int i = lane; i < m; i += 32) {
+          double kr, ki;
+          proxy_entry<OP, RAND>(a, c, plen, pts, i, xj, gj, kr, ki);
+          col[i * W] = kr;
+          if (C) col[i * W + 1] = ki;
+          bad |= !isfinite(kr) || (C && !isfinite(ki));
+        }
       }
       if (bad && a.nonfinite) *a.nonfinite = 1;
     }
   }
   __syncthreads();
+  // K(row, column j) as FP64 (either storage)
+  auto kval = [&](int j, int row) -> double {
+    return pairs ? pair_to_f64(reinterpret_cast<const float2*>(A)[(int64_t)j * m + row])
+                 : A[((int64_t)j * m + row) * W];
+  };
 
   double* T = a.t_out + a.t_off_out[b] * W;
   int rank = 0;
@@ -708,6 +793,21 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
         double yr = 0, yi = 0;
         const double* col = A + (int64_t)j * m * W;
         const int32_t* row = a.sk_tab + (int64_t)t * a.rho;
+        if (pairs) {
+          // signed sum of FP32 pairs, compensated in FP32 (TwoSum)
+          const float2* colp = reinterpret_cast<const float2*>(col);
+          float sh = 0.f, sl = 0.f;
+          for (int u = 0; u < a.rho; ++u) {
+            const int32_t e = row[u];
+            float2 v = colp[e & 0x7fffffff];
+            if (e < 0) v = make_float2(-v.x, -v.y);
+            float err;
+            two_sum_f(sh, v.x, sh, err);
+            sl = __fadd_rn(sl, __fadd_rn(err, v.y));
+          }
+          Y[(int64_t)j * s + t] = pair_to_f64(make_float2(sh, sl));
+          continue;
+        }
         for (int u = 0; u < a.rho; ++u) {
           const int32_t e = row[u];
           const int i = e & 0x7fffffff;
@@ -736,13 +836,13 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
         const int row = (int)__umulhi((unsigned)(mix64(key ^ (0xC0FFEEull + (uint64_t)qi)) >> 32), (unsigned)m);
         for (int jr = threadIdx.x; jr < n; jr += blockDim.x) {
           const int pj = q.piv[jr];
-          const double zr = A[((int64_t)pj * m + row) * W], zi = C ? A[((int64_t)pj * m + row) * W + 1] : 0.0;
+          const double zr = kval(pj, row), zi = C ? A[((int64_t)pj * m + row) * W + 1] : 0.0;
           z2 += zr * zr + zi * zi;
           if (jr < rank) continue;
           double er = zr, ei = zi;
           for (int i = 0; i < rank; ++i) {
             const int pi = q.piv[i];
-            const double sr = A[((int64_t)pi * m + row) * W], si = C ? A[((int64_t)pi * m + row) * W + 1] : 0.0;
+            const double sr = kval(pi, row), si = C ? A[((int64_t)pi * m + row) * W + 1] : 0.0;
             const double tr = T[((int64_t)i * nr + (jr - rank)) * W];
             const double ti = C ? T[((int64_t)i * nr + (jr - rank)) * W + 1] : 0.0;
             er -= sr * tr - si * ti;
@@ -767,6 +867,14 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
   }
   if (!done) {
     if (a.defer) return;
+    if (pairs) {
+      // K back to FP64 in place (each thread converts its own entries)
+      for (int64_t idx = threadIdx.x; idx < (int64_t)m * n; idx += blockDim.x) {
+        const float2 v = reinterpret_cast<const float2*>(A)[idx];
+        A[idx] = pair_to_f64(v);
+      }
+      __syncthreads();
+    }
     // ---- 3. full column-pivoted QR ID of K
     rank = pivoted_qr<OP>(A, m, n, a.tol >= 1.0 ? 0.0 : a.tol, a.tol >= 1.0 ? (int)a.tol : 0, q);
     write_T<OP>(A, m, n, rank, T, q.vn1);

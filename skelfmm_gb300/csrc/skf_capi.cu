@@ -85,6 +85,112 @@ static void free_plan(skf_plan* p) {
   delete p;
 }
 
+// ---- entry preparation and list checks on the device (plan creation)
+constexpr int kPrepThreads = 256;
+constexpr int kPrepBlocks = 304;  // 2 per SM on 152 SMs
+
+// Per block: min and max of every coordinate (part[6 b + k], part[6 b + 3 +
+// k]); *bad = 1 when a coordinate or normal is not finite.
+__global__ void __launch_bounds__(kPrepThreads) k_entry_minmax(int64_t E, int ndim, const double* __restrict__ xyz,
+                                                               const double* __restrict__ geom,
+                                                               double* __restrict__ part, int* bad) {
+  __shared__ double smin[3][kPrepThreads], smax[3][kPrepThreads];
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  bool nf = false;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    for (int k = 0; k < ndim; ++k) {
+      const double c = xyz[e * ndim + k];
+      nf |= !isfinite(c);
+      lo[k] = fmin(lo[k], c);
+      hi[k] = fmax(hi[k], c);
+    }
+    if (geom) nf |= !(isfinite(geom[3 * e]) && isfinite(geom[3 * e + 1]) && isfinite(geom[3 * e + 2]));
+  }
+  if (nf) *bad = 1;
+  for (int k = 0; k < 3; ++k) {
+    smin[k][threadIdx.x] = lo[k];
+    smax[k][threadIdx.x] = hi[k];
+  }
+  __syncthreads();
+  for (int w = kPrepThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int k = 0; k < 3; ++k) {
+        smin[k][threadIdx.x] = fmin(smin[k][threadIdx.x], smin[k][threadIdx.x + w]);
+        smax[k][threadIdx.x] = fmax(smax[k][threadIdx.x], smax[k][threadIdx.x + w]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; ++k) {
+      part[6 * blockIdx.x + k] = smin[k][0];
+      part[6 * blockIdx.x + 3 + k] = smax[k][0];
+    }
+}
+
+// FP64 (x, y, z, 0) of every entry and the FP32 split of s = (x - cmin) + B
+// (hi = fl32(s), lo = fl32(s - hi)); normals as FP64 and as an FP32 pair.
+__global__ void k_entry_pack(int64_t E, int ndim, const double* __restrict__ xyz, const double* __restrict__ geom,
+                             double cx, double cy, double cz, double B, double4_32a* __restrict__ xyz64,
+                             float4* __restrict__ hi, float4* __restrict__ lo, double4_32a* __restrict__ g64,
+                             float4* __restrict__ g32, float4* __restrict__ g32lo) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const double cmin[3] = {cx, cy, cz};
+  double c[3] = {0, 0, 0};
+  float h[3] = {0, 0, 0}, l[3] = {0, 0, 0};
+  for (int k = 0; k < ndim; ++k) {
+    c[k] = xyz[e * ndim + k];
+    const double sk = __dadd_rn(__dsub_rn(c[k], cmin[k]), B);
+    h[k] = __double2float_rn(sk);
+    l[k] = __double2float_rn(__dsub_rn(sk, (double)h[k]));
+  }
+  xyz64[e] = make_double4_32a(c[0], c[1], c[2], 0.0);
+  hi[e] = make_float4(h[0], h[1], h[2], 0.f);
+  lo[e] = make_float4(l[0], l[1], l[2], 0.f);
+  if (geom) {
+    const double gx = geom[3 * e], gy = geom[3 * e + 1], gz = geom[3 * e + 2];
+    g64[e] = make_double4_32a(gx, gy, gz, 0.0);
+    const float fx = __double2float_rn(gx), fy = __double2float_rn(gy), fz = __double2float_rn(gz);
+    g32[e] = make_float4(fx, fy, fz, 0.f);
+    g32lo[e] = make_float4(__double2float_rn(__dsub_rn(gx, (double)fx)), __double2float_rn(__dsub_rn(gy, (double)fy)),
+                           __double2float_rn(__dsub_rn(gz, (double)fz)), 0.f);
+  }
+}
+
+__device__ __forceinline__ int mirror_kind(int k) {
+  return k == SKF_KIND_COARSE_UP ? SKF_KIND_COARSE_DOWN : (k == SKF_KIND_COARSE_DOWN ? SKF_KIND_COARSE_UP : k);
+}
+
+// *bad = 1 when a box lists a source twice, or lists (B, kind), B != A,
+// without B listing (A, mirror kind).  One thread per list entry.
+__global__ void k_sym_check(int nb, int64_t L, const int64_t* __restrict__ off, const int32_t* __restrict__ src,
+                            const int8_t* __restrict__ kind, int* bad) {
+  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L) return;
+  int lo = 0, hi = nb;  // A = the box whose list holds entry l
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= l)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const int A = lo, B = src[l];
+  for (int64_t k = off[A]; k < l; ++k)
+    if (src[k] == B) {
+      *bad = 1;
+      return;
+    }
+  if (B == A) return;
+  const int want = mirror_kind(kind[l]);
+  for (int64_t k = off[B]; k < off[B + 1]; ++k)
+    if (src[k] == A) {
+      if (kind[k] != want) *bad = 1;
+      return;
+    }
+  *bad = 1;
+}
+
 }  // namespace skf
 
 using namespace skf;
@@ -170,67 +276,101 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   p->nlist = L;
   for (int b = 0; b < nb; ++b) p->max_bs = std::max<int>(p->max_bs, (int)(d->box_off[b + 1] - d->box_off[b]));
 
-  for (int64_t e = 0; e < E * d->ndim; ++e)
-    if (!std::isfinite(d->entry_xyz[e])) {
-      free_plan(p);
-      return SKF_ERR_ARG;
-    }
-  if (d->entry_geom)
-    for (int64_t e = 0; e < E * 3; ++e)
-      if (!std::isfinite(d->entry_geom[e])) {
+  if (!d->entries_on_device) {
+    // host entries are checked here, before any device work
+    for (int64_t e = 0; e < E * d->ndim; ++e)
+      if (!std::isfinite(d->entry_xyz[e])) {
         free_plan(p);
         return SKF_ERR_ARG;
       }
-  // entry coordinates: FP64 (x,y,z,0) and the FP32 hi/lo split.  The split
-  // is taken of the coordinates translated into one binade [B, 2B), B a power
-  // of two above the extent of the entries: every hi then lies on the same
-  // FP32 grid (spacing B 2^-23), so hi_i - hi_j is exact for every pair and
-  // d = (hi_i - hi_j) + (lo_i - lo_j) carries d to ~B 2^-48 absolute.  The
-  // kernels only use differences, so the translation changes nothing else.
-  double cmin[3] = {0, 0, 0}, cmax[3] = {0, 0, 0};
-  for (int k = 0; k < d->ndim; ++k) {
-    cmin[k] = cmax[k] = d->entry_xyz[k];
-    for (int64_t e = 1; e < E; ++e) {
-      const double c = d->entry_xyz[e * d->ndim + k];
-      cmin[k] = std::min(cmin[k], c);
-      cmax[k] = std::max(cmax[k], c);
-    }
+    if (d->entry_geom)
+      for (int64_t e = 0; e < E * 3; ++e)
+        if (!std::isfinite(d->entry_geom[e])) {
+          free_plan(p);
+          return SKF_ERR_ARG;
+        }
   }
-  double extent = 0.0;
-  for (int k = 0; k < d->ndim; ++k) extent = std::max(extent, cmax[k] - cmin[k]);
-  const double B = extent > 0.0 ? std::ldexp(1.0, std::ilogb(extent) + 1) : 1.0;
-  std::vector<double4_32a> xyz(E);
-  std::vector<float4> hi(E), lo(E);
-  for (int64_t e = 0; e < E; ++e) {
-    double c[3] = {0, 0, 0};
-    for (int k = 0; k < d->ndim; ++k) c[k] = d->entry_xyz[e * d->ndim + k];
-    xyz[e] = make_double4_32a(c[0], c[1], c[2], 0.0);
-    float h[3] = {0, 0, 0}, l[3] = {0, 0, 0};
-    for (int k = 0; k < d->ndim; ++k) {
-      const double s = (c[k] - cmin[k]) + B;
-      h[k] = (float)s;
-      l[k] = (float)(s - (double)h[k]);
+  // entry coordinates: FP64 (x,y,z,0) and the FP32 hi/lo split, prepared on
+  // the device.  The split is taken of the coordinates translated into one
+  // binade [B, 2B), B a power of two above the extent of the entries: every
+  // hi then lies on the same FP32 grid (spacing B 2^-23), so hi_i - hi_j is
+  // exact for every pair and d = (hi_i - hi_j) + (lo_i - lo_j) carries d to
+  // ~B 2^-48 absolute.  The kernels only use differences, so the
+  // translation changes nothing else.  Normals: FP64 and an FP32 pair (hi =
+  // fl32(n), lo = fl32(n - hi)); the double-layer kernels form (x - y).n
+  // from the pair (see dot_dn).  A non-finite coordinate or normal on the
+  // device is rejected (SKF_ERR_ARG) before anything else is uploaded.
+  {
+    const int D = d->ndim;
+    const double* xin = d->entry_xyz;
+    const double* gin = d->entry_geom;
+    double* scratch = nullptr;  // raw host entries staged on the device
+    if (!d->entries_on_device) {
+      const size_t nx = (size_t)E * D, ng = d->entry_geom ? (size_t)E * 3 : 0;
+      cudaError_t e = cudaMalloc(&scratch, sizeof(double) * (nx + ng));
+      if (e == cudaSuccess) e = cudaMemcpy(scratch, d->entry_xyz, sizeof(double) * nx, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess && ng) e = cudaMemcpy(scratch + nx, d->entry_geom, sizeof(double) * ng, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        cudaFree(scratch);
+        set_last_cuda_error(e);
+        free_plan(p);
+        return e == cudaErrorMemoryAllocation ? SKF_ERR_OOM : SKF_ERR_CUDA;
+      }
+      xin = scratch;
+      gin = ng ? scratch + nx : nullptr;
     }
-    hi[e] = make_float4(h[0], h[1], h[2], 0.f);
-    lo[e] = make_float4(l[0], l[1], l[2], 0.f);
-  }
-  SKF_TRY(upload(p, &p->xyz64, xyz.data(), E));
-  SKF_TRY(upload(p, &p->hi32, hi.data(), E));
-  SKF_TRY(upload(p, &p->lo32, lo.data(), E));
-  if (d->entry_geom) {
-    // normals as FP64 and as an FP32 pair (hi = fl32(n), lo = fl32(n - hi)):
-    // the double-layer kernels form (x - y).n from the pair (see dot_dn)
-    std::vector<double4_32a> g(E);
-    std::vector<float4> g32(E), g32lo(E);
-    for (int64_t e = 0; e < E; ++e) {
-      g[e] = make_double4_32a(d->entry_geom[3 * e], d->entry_geom[3 * e + 1], d->entry_geom[3 * e + 2], 0.0);
-      g32[e] = make_float4((float)g[e].x, (float)g[e].y, (float)g[e].z, 0.f);
-      g32lo[e] = make_float4((float)(g[e].x - (double)g32[e].x), (float)(g[e].y - (double)g32[e].y),
-                             (float)(g[e].z - (double)g32[e].z), 0.f);
+    double* part = nullptr;
+    int* dbad = nullptr;
+    std::vector<double> hpart(6 * kPrepBlocks);
+    int hbad = 0;
+    cudaError_t e = cudaMalloc(&part, sizeof(double) * 6 * kPrepBlocks);
+    if (e == cudaSuccess) e = cudaMalloc(&dbad, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(dbad, 0, sizeof(int));
+    if (e == cudaSuccess) {
+      k_entry_minmax<<<kPrepBlocks, kPrepThreads>>>(E, D, xin, gin, part, dbad);
+      e = cudaGetLastError();
     }
-    SKF_TRY(upload(p, &p->geom64, g.data(), E));
-    SKF_TRY(upload(p, &p->geom32, g32.data(), E));
-    SKF_TRY(upload(p, &p->geom32lo, g32lo.data(), E));
+    if (e == cudaSuccess) e = cudaMemcpy(hpart.data(), part, sizeof(double) * 6 * kPrepBlocks, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(part);
+    cudaFree(dbad);
+    if (e != cudaSuccess || hbad) {
+      cudaFree(scratch);
+      if (e != cudaSuccess) set_last_cuda_error(e);
+      free_plan(p);
+      return e != cudaSuccess ? SKF_ERR_CUDA : SKF_ERR_ARG;
+    }
+    double cmin[3] = {0, 0, 0}, cmax[3] = {0, 0, 0};
+    for (int k = 0; k < D; ++k) {
+      cmin[k] = hpart[k];
+      cmax[k] = hpart[3 + k];
+      for (int b = 1; b < kPrepBlocks; ++b) {
+        cmin[k] = std::min(cmin[k], hpart[6 * b + k]);
+        cmax[k] = std::max(cmax[k], hpart[6 * b + 3 + k]);
+      }
+    }
+    double extent = 0.0;
+    for (int k = 0; k < D; ++k) extent = std::max(extent, cmax[k] - cmin[k]);
+    const double B = extent > 0.0 ? std::ldexp(1.0, std::ilogb(extent) + 1) : 1.0;
+    int st = upload(p, &p->xyz64, (const double4_32a*)nullptr, E);
+    if (st == SKF_OK) st = upload(p, &p->hi32, (const float4*)nullptr, E);
+    if (st == SKF_OK) st = upload(p, &p->lo32, (const float4*)nullptr, E);
+    if (st == SKF_OK && gin) st = upload(p, &p->geom64, (const double4_32a*)nullptr, E);
+    if (st == SKF_OK && gin) st = upload(p, &p->geom32, (const float4*)nullptr, E);
+    if (st == SKF_OK && gin) st = upload(p, &p->geom32lo, (const float4*)nullptr, E);
+    if (st == SKF_OK) {
+      k_entry_pack<<<(unsigned)((E + kPrepThreads - 1) / kPrepThreads), kPrepThreads>>>(
+          E, D, xin, gin, cmin[0], cmin[1], cmin[2], B, p->xyz64, p->hi32, p->lo32, p->geom64, p->geom32,
+          p->geom32lo);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) {
+        set_last_cuda_error(e);
+        st = SKF_ERR_CUDA;
+      }
+    }
+    cudaFree(scratch);
+    SKF_TRY(st);
   }
   SKF_TRY(upload(p, &p->box_off, d->box_off, (size_t)nb + 1));
   SKF_TRY(upload(p, &p->box_rank, d->box_rank, (size_t)nb));
@@ -330,29 +470,27 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   if (d->op == SKF_LAPLACE_2D || d->op == SKF_LAPLACE_3D || d->op == SKF_HELMHOLTZ_3D) {
     // partial arrays per owned entry: u, uh (real); u re/im, uh re/im (complex)
     const int nparts = cplx ? 4 : 2;
-    auto mirror = [](int k) {
-      return k == SKF_KIND_COARSE_UP ? SKF_KIND_COARSE_DOWN : (k == SKF_KIND_COARSE_DOWN ? SKF_KIND_COARSE_UP : k);
-    };
-    // each box's list sorted by source: no source twice, and every (A, B,
-    // kind) has its (B, A, mirror kind) in B's list (binary search)
-    std::vector<std::pair<int32_t, int8_t>> sorted_lists((size_t)L);
-    for (int64_t l = 0; l < L; ++l) sorted_lists[l] = {d->list_src[l], d->list_kind[l]};
+    // no box lists a source twice, and every (A, B, kind) has its (B, A,
+    // mirror kind) in B's list (checked on the device)
     bool ok = true;
-    for (int A = 0; A < nb && ok; ++A) {
-      auto b = sorted_lists.begin() + d->list_off[A], e = sorted_lists.begin() + d->list_off[A + 1];
-      std::sort(b, e);
-      for (auto it = b; it + 1 < e; ++it)
-        if (it->first == (it + 1)->first) ok = false;
-    }
-    for (int A = 0; A < nb && ok; ++A)
-      for (int64_t l = d->list_off[A]; l < d->list_off[A + 1] && ok; ++l) {
-        const int B = sorted_lists[l].first;
-        if (B == A) continue;
-        auto b = sorted_lists.begin() + d->list_off[B], e = sorted_lists.begin() + d->list_off[B + 1];
-        auto m = std::lower_bound(b, e, std::make_pair((int32_t)A, (int8_t)INT8_MIN));
-        if (m == e || m->first != A || m->second != mirror(sorted_lists[l].second)) ok = false;
+    if (L > 0) {
+      int* dbad = nullptr;
+      int hbad = 0;
+      cudaError_t e = cudaMalloc(&dbad, sizeof(int));
+      if (e == cudaSuccess) e = cudaMemset(dbad, 0, sizeof(int));
+      if (e == cudaSuccess) {
+        k_sym_check<<<(unsigned)((L + 255) / 256), 256>>>(nb, L, p->list_off, p->list_src, p->list_kind, dbad);
+        e = cudaGetLastError();
       }
-    std::vector<std::pair<int32_t, int8_t>>().swap(sorted_lists);
+      if (e == cudaSuccess) e = cudaMemcpy(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost);
+      cudaFree(dbad);
+      if (e != cudaSuccess) {
+        set_last_cuda_error(e);
+        free_plan(p);
+        return SKF_ERR_CUDA;
+      }
+      ok = hbad == 0;
+    }
     if (ok) {
       const int tile = kT32Threads * kRowsPerThreadF32;
       std::vector<int64_t> soff(nb + 1, 0), poff, pbase(nb, 0), pstride(nb, 0);

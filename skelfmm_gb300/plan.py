@@ -32,8 +32,8 @@ class RaggedBuild:
     box_level: np.ndarray   # int32 [nb]
     box_off: np.ndarray     # int64 [nb+1]
     box_rank: np.ndarray    # int32 [nb]
-    entry_xyz: np.ndarray   # f64 [E, ndim]
-    entry_geom: np.ndarray | None  # f64 [E, 3]
+    entry_xyz: np.ndarray   # f64 [E, ndim] (numpy, or a CUDA tensor)
+    entry_geom: np.ndarray | None  # f64 [E, 3] (numpy, or a CUDA tensor)
     entry_pslot: np.ndarray  # int64 [E]
     perm_entry: np.ndarray   # int64 [N]
     perm_point: np.ndarray   # int64 [N]
@@ -164,18 +164,24 @@ _DTYPES = {"box_level": np.int32, "box_off": np.int64, "box_rank": np.int32, "en
            "list_off": np.int64, "list_src": np.int32, "list_kind": np.int8}
 
 
+def host_array(a):
+    """``a`` as a numpy array (device tensors copied to the host)."""
+    return a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else a
+
+
 def save_ragged(rb: RaggedBuild, path, extra=None):
-    """Write ``rb`` (T copied to the host if it is on the device) to ``path``
-    (.npz).  ``extra``: further named arrays stored beside it."""
-    t = rb.t_data.detach().cpu().numpy() if isinstance(rb.t_data, torch.Tensor) else np.asarray(rb.t_data)
+    """Write ``rb`` (T and entries copied to the host if they are on the
+    device) to ``path`` (.npz).  ``extra``: further named arrays stored
+    beside it."""
+    t = np.asarray(host_array(rb.t_data))
     out = {"format": np.array(FORMAT_TAG), "version": np.array(FORMAT_VERSION),
            "t_dtype": np.array(str(t.dtype)),
            "scalars": np.array([rb.op, rb.ndim, rb.npoints, rb.nlevels, rb.root_level], dtype=np.int64),
            "kappa": np.array(rb.kappa, dtype=np.float64)}
     for k in _ARRAYS:
-        out[k] = t if k == "t_data" else np.ascontiguousarray(getattr(rb, k), dtype=_DTYPES[k])
+        out[k] = t if k == "t_data" else np.ascontiguousarray(host_array(getattr(rb, k)), dtype=_DTYPES[k])
     if rb.entry_geom is not None:
-        out["entry_geom"] = np.ascontiguousarray(rb.entry_geom, dtype=np.float64)
+        out["entry_geom"] = np.ascontiguousarray(host_array(rb.entry_geom), dtype=np.float64)
     for k, v in (extra or {}).items():
         out["extra/" + k] = np.asarray(v)
     with open(path, "wb") as f:
@@ -239,8 +245,26 @@ class Plan:
         d.box_level = arr("box_level", rb.box_level, np.int32)
         d.box_off = arr("box_off", rb.box_off, np.int64)
         d.box_rank = arr("box_rank", rb.box_rank, np.int32)
-        d.entry_xyz = arr("entry_xyz", rb.entry_xyz, np.float64)
-        d.entry_geom = None if rb.entry_geom is None else arr("entry_geom", rb.entry_geom, np.float64)
+        if isinstance(rb.entry_xyz, torch.Tensor):
+            # entries already on the device (a build's own gather): used in place
+            def dev(name, a):
+                if a is None:
+                    return None
+                if not a.is_cuda or a.dtype != torch.float64:
+                    raise ValueError(f"device {name} must be a CUDA float64 tensor")
+                a = a.contiguous()
+                keep[name] = a
+                return a.data_ptr()
+
+            if rb.entry_geom is not None and not isinstance(rb.entry_geom, torch.Tensor):
+                raise ValueError("entry_geom must live where entry_xyz does")
+            d.entry_xyz = dev("entry_xyz", rb.entry_xyz)
+            d.entry_geom = dev("entry_geom", rb.entry_geom)
+            d.entries_on_device = 1
+        else:
+            d.entry_xyz = arr("entry_xyz", rb.entry_xyz, np.float64)
+            d.entry_geom = None if rb.entry_geom is None else arr("entry_geom", rb.entry_geom, np.float64)
+            d.entries_on_device = 0
         d.entry_pslot = arr("entry_pslot", rb.entry_pslot, np.int64)
         d.nperm = int(rb.perm_entry.shape[0])
         d.perm_entry = arr("perm_entry", rb.perm_entry, np.int64)
@@ -312,13 +336,14 @@ class Plan:
     def autotune(self, precision=_lib.PREC_MIXED, reps=3, exhaustive=False):
         """Time translation schemes this plan supports and keep the fastest.
 
-        Candidates: the source-split symmetric kernel and the 64-source tile
-        of the block-barrier symmetric kernel (Laplace) or its 64 and
-        32-source tiles (Helmholtz 3D), when the lists are symmetric, and the
-        per-direction packed kernel's 4-warp and 2-warp shapes; with
-        ``exhaustive`` every shape of both kernels.  Each candidate is timed
-        once, then the two fastest ``reps`` times.  Returns {(symmetric,
-        shape): ms}; the choice is kept in ``self.tuned``."""
+        Candidates: for real operators the source-split symmetric kernel
+        (when the lists are symmetric) and the per-direction packed kernel's
+        4-warp shape; for Helmholtz 3D the block-barrier symmetric kernel's
+        64 and 32-source tiles and the packed kernel's 4-warp and 2-warp
+        shapes; with ``exhaustive`` every shape of both kernels.  Each
+        candidate is timed once, then the two fastest ``reps`` times unless
+        the fastest leads by more than 15 %.  Returns {(symmetric, shape):
+        ms}; the choice is kept in ``self.tuned``."""
         self.set_option(_lib.OPT_SYMMETRIC, 1)
         info = self._query()
         sym_ok = info.npairs_evaluated_mixed < info.npairs_fused
@@ -326,7 +351,7 @@ class Plan:
             # shapes 4 and 5: the source-split Laplace kernel (grid, persistent queue)
             sym_shapes, dir_shapes = (range(4) if self.is_complex else range(6)), range(3)
         else:
-            sym_shapes, dir_shapes = ((0, 2) if self.is_complex else (4, 0)), (0, 2)
+            sym_shapes, dir_shapes = ((0, 2), (0, 2)) if self.is_complex else ((4,), (0,))
         cands = ([(1, sh) for sh in sym_shapes] if sym_ok else []) + [(0, sh) for sh in dir_shapes]
 
         def select(sym, shape):
@@ -342,7 +367,9 @@ class Plan:
                 self.time_translations(precision, reps=1)
                 _WARMED.add(key)
             results[(sym, shape)] = self.time_translations(precision, reps=1)
-        for cand in sorted(results, key=results.get)[:2]:
+        top = sorted(results, key=results.get)[:2]
+        clear = len(top) < 2 or results[top[1]] > 1.15 * results[top[0]]
+        for cand in ([] if clear else top):
             if results[cand] < 20.0:
                 # long launches keep the single timing: their spread is well
                 # below the differences between schemes

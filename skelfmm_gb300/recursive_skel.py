@@ -503,13 +503,18 @@ class RecursiveSkeletonization:
             print("\t root level %d, %d root boxes, %d entries" % (self.root_level, root_boxes.shape[0], off[-1]))
 
     def _gather_xyz(self, pid):
-        """Coordinates of the points ``pid`` (host float64 [len, ndim]),
+        """Coordinates of the points ``pid`` (device float64 [len, ndim]),
         gathered from the build's device copy."""
         idx = torch.from_numpy(np.ascontiguousarray(pid, dtype=np.int64)).to(self.device)
-        return self._XX_dev.index_select(0, idx).cpu().numpy()
+        return self._XX_dev.index_select(0, idx)
 
     def ragged(self):
-        geom = None if self.geometry is None else self.geometry[self.entry_pid]
+        """The build as a ``RaggedBuild``; T and the entries' coordinates
+        (and normals) stay on the device."""
+        geom = None
+        if self._geom_dev is not None:
+            idx = torch.from_numpy(np.ascontiguousarray(self.entry_pid, dtype=np.int64)).to(self.device)
+            geom = self._geom_dev.index_select(0, idx)
         return RaggedBuild(
             op=self.op_id, ndim=self.ndim, kappa=self.kappa, npoints=int(self.N), nlevels=int(self.nlevels),
             root_level=int(self.root_level), box_level=self.tree.get_boxes_levels().astype(np.int32),
