@@ -583,8 +583,10 @@ def run_batch(args):
     torch.cuda.set_device(dev)
     pts, xs = batch_instances(seed=rank)
     ntot = int(sum(p.shape[0] for p in pts))
-    SkelFMMBatch([get_point_dist(5000, "curvy_annulus", rng=np.random.default_rng(9))], operators.LAPLACE_2D,
-                 tune=False)
+    # warm-up build over the instance size range (first use of each kernel,
+    # including the device sort's large-array path)
+    SkelFMMBatch([get_point_dist(n, "curvy_annulus", rng=np.random.default_rng(9)) for n in (5000, 200000)],
+                 operators.LAPLACE_2D, tune=False)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     b = SkelFMMBatch(pts, operators.LAPLACE_2D, tol=1e-6, leaf_size=128, precision="mixed", tune=True)

@@ -1178,6 +1178,21 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
   double c[3] = {0, 0, 0};
   for (int d = 0; d < D; ++d) c[d] = a.centers[(int64_t)b * D + d];
   const double plen = a.box_len ? 2.95 * a.box_len[b] : a.plen;
+  // randomized 3D Laplace: K from FP32-pair entries (lap3d_pair, relative
+  // error ~1e-13), rounded to FP64 (the fallback factors K in place)
+  constexpr bool kPairs = RAND && OP == SKF_LAPLACE_3D;
+  const bool pairs = kPairs && m == a.np;
+  float* vh = reinterpret_cast<float*>(s.posof + n);
+  float* vl = vh + 3 * a.np;
+  if (pairs) {
+    for (int i = threadIdx.x; i < a.np * 3; i += blockDim.x) {
+      const double v = plen * a.tmpl[i];
+      const float h = __double2float_rn(v);
+      vh[i] = h;
+      vl[i] = __double2float_rn(v - (double)h);
+    }
+    __syncthreads();
+  }
 
   // ---- proxy matrix, owned columns only (a warp per column)
   for (int jl = warp; jl < ncl; jl += nw) {
@@ -1188,11 +1203,25 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
     bool bad = false;
     for (int d = 0; d < D; ++d) bad |= !isfinite(xj[d]);
     if (gj) bad |= !(isfinite(gj[0]) && isfinite(gj[1]) && isfinite(gj[2]));
-    for (int i = lane; i < m; i += 32) {
-      double kr, ki;
-      proxy_entry<OP>(a, c, plen, nullptr, i, xj, gj, kr, ki);
-      A[(int64_t)j * m + i] = kr;
-      bad |= !isfinite(kr);
+    if (pairs) {
+      float uh[3], ul[3];
+      for (int d = 0; d < 3; ++d) {
+        const double u = xj[d] - c[d];
+        uh[d] = __double2float_rn(u);
+        ul[d] = __double2float_rn(u - (double)uh[d]);
+      }
+      for (int i = lane; i < m; i += 32) {
+        const float2 k = lap3d_pair(uh, ul, vh + 3 * i, vl + 3 * i);
+        A[(int64_t)j * m + i] = pair_to_f64(k);
+        bad |= !isfinite(k.x);
+      }
+    } else {
+      for (int i = lane; i < m; i += 32) {
+        double kr, ki;
+        proxy_entry<OP>(a, c, plen, nullptr, i, xj, gj, kr, ki);
+        A[(int64_t)j * m + i] = kr;
+        bad |= !isfinite(kr);
+      }
     }
     if (bad && a.nonfinite) *a.nonfinite = 1;
   }
@@ -1308,7 +1337,9 @@ static int launch_skel_cluster_t(const SkelArgs& a, int nbox, size_t smem, cudaS
 template <int OP>
 static int launch_skel_cluster(const SkelArgs& a, int nbox, int maxn, cudaStream_t st) {
   const int ncl = (maxn + kClusterCTAs - 1) / kClusterCTAs;
-  const size_t smem = sizeof(double) * ((size_t)2 * a.mrows + 64 + 8 + 2 * (size_t)ncl) + sizeof(int) * 2 * (size_t)maxn;
+  size_t smem = sizeof(double) * ((size_t)2 * a.mrows + 64 + 8 + 2 * (size_t)ncl) + sizeof(int) * 2 * (size_t)maxn;
+  // randomized 3D Laplace: the proxies relative to the centre as FP32 pairs
+  if (a.kpred && OP == SKF_LAPLACE_3D) smem += sizeof(float) * 6 * (size_t)a.np;
   if (smem > 200 * 1024) return SKF_ERR_UNSUPPORTED;
   return a.kpred ? launch_skel_cluster_t<OP, true>(a, nbox, smem, st) : launch_skel_cluster_t<OP, false>(a, nbox, smem, st);
 }
