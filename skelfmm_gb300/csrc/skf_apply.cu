@@ -179,6 +179,29 @@ __device__ __forceinline__ double ff_warp_sum(FF a) {
   }
   return (double)a.s + (double)a.c;
 }
+// Sum of float-float values over aligned groups of g lanes (g a power of
+// two): every lane of a group holds the group's sum, in a fixed order.
+__device__ __forceinline__ FF ff_group_sum(FF a, int g) {
+  for (int o = g >> 1; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, a.s, o);
+    const float c2 = __shfl_xor_sync(0xffffffffu, a.c, o);
+    const float t = a.s + s2;
+    const float z = t - a.s;
+    const float err = (a.s - (t - z)) + (s2 - z);
+    a.s = t;
+    a.c = (a.c + c2) + err;
+  }
+  return a;
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float t = a.s + b.s;
+  const float z = t - a.s;
+  const float err = (a.s - (t - z)) + (b.s - z);
+  FF r;
+  r.s = t;
+  r.c = (a.c + b.c) + err;
+  return r;
+}
 __device__ __forceinline__ void split_f64(double v, float& h, float& l) {
   h = (float)v;
   l = (float)(v - (double)h);
@@ -204,25 +227,58 @@ __global__ void __launch_bounds__(256) k_up_ff(const int32_t* __restrict__ boxes
   const float* Th = thi + t_off[b] * W;
   const float* Tl = tlo + t_off[b] * W;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int i = warp; i < r; i += nw) {
-    const int64_t rb = (int64_t)i * nred * W;
-    FF ar, ai;
-    for (int c = lane; c < nred; c += 32) {
-      if (C) {
-        const float trh = Th[rb + 2 * c], tih = Th[rb + 2 * c + 1];
-        const float trl = Tl[rb + 2 * c], til = Tl[rb + 2 * c + 1];
-        const float xrh = xh[2 * c], xih = xh[2 * c + 1], xrl = xl[2 * c], xil = xl[2 * c + 1];
-        ff_add_prod(ar, trh, trl, xrh, xrl);
-        ff_sub_prod(ar, tih, til, xih, xil);
-        ff_add_prod(ai, trh, trl, xih, xil);
-        ff_add_prod(ai, tih, til, xrh, xrl);
-      } else {
-        ff_add_prod(ar, Th[rb + c], Tl[rb + c], xh[c], xl[c]);
+  // g lanes per row (about 8+ columns a lane), 32 / g rows per warp; two
+  // accumulators per lane (alternate column strides) for independent chains
+  const int g = nred > 256 ? 32 : (nred > 128 ? 16 : (nred > 32 ? 8 : 4));
+  const int rows = 32 / g, lg = lane & (g - 1);
+  for (int i0 = warp * rows; i0 < r; i0 += nw * rows) {
+    const int i = i0 + lane / g;
+    const int64_t rb = (int64_t)min(i, r - 1) * nred * W;
+    FF ar, ai, br, bi;
+    if (i < r) {
+      int c = lg;
+      for (; c + g < nred; c += 2 * g) {
+        if (C) {
+          const float trh = Th[rb + 2 * c], tih = Th[rb + 2 * c + 1];
+          const float trl = Tl[rb + 2 * c], til = Tl[rb + 2 * c + 1];
+          const float xrh = xh[2 * c], xih = xh[2 * c + 1], xrl = xl[2 * c], xil = xl[2 * c + 1];
+          const int d = c + g;
+          const float urh = Th[rb + 2 * d], uih = Th[rb + 2 * d + 1];
+          const float url = Tl[rb + 2 * d], uil = Tl[rb + 2 * d + 1];
+          const float yrh = xh[2 * d], yih = xh[2 * d + 1], yrl = xl[2 * d], yil = xl[2 * d + 1];
+          ff_add_prod(ar, trh, trl, xrh, xrl);
+          ff_sub_prod(ar, tih, til, xih, xil);
+          ff_add_prod(ai, trh, trl, xih, xil);
+          ff_add_prod(ai, tih, til, xrh, xrl);
+          ff_add_prod(br, urh, url, yrh, yrl);
+          ff_sub_prod(br, uih, uil, yih, yil);
+          ff_add_prod(bi, urh, url, yih, yil);
+          ff_add_prod(bi, uih, uil, yrh, yrl);
+        } else {
+          const float t0h = Th[rb + c], t0l = Tl[rb + c], t1h = Th[rb + c + g], t1l = Tl[rb + c + g];
+          ff_add_prod(ar, t0h, t0l, xh[c], xl[c]);
+          ff_add_prod(br, t1h, t1l, xh[c + g], xl[c + g]);
+        }
+      }
+      if (c < nred) {
+        if (C) {
+          const float trh = Th[rb + 2 * c], tih = Th[rb + 2 * c + 1];
+          const float trl = Tl[rb + 2 * c], til = Tl[rb + 2 * c + 1];
+          const float xrh = xh[2 * c], xih = xh[2 * c + 1], xrl = xl[2 * c], xil = xl[2 * c + 1];
+          ff_add_prod(ar, trh, trl, xrh, xrl);
+          ff_sub_prod(ar, tih, til, xih, xil);
+          ff_add_prod(ai, trh, trl, xih, xil);
+          ff_add_prod(ai, tih, til, xrh, xrl);
+        } else {
+          ff_add_prod(ar, Th[rb + c], Tl[rb + c], xh[c], xl[c]);
+        }
       }
     }
-    const double sr = ff_warp_sum(ar);
-    const double si = C ? ff_warp_sum(ai) : 0.0;
-    if (lane == 0) {
+    const FF tr = ff_group_sum(ff_add(ar, br), g);
+    const FF ti = C ? ff_group_sum(ff_add(ai, bi), g) : FF();
+    const double sr = (double)tr.s + (double)tr.c;
+    const double si = C ? (double)ti.s + (double)ti.c : 0.0;
+    if (lg == 0 && i < r) {
       const int64_t e = off + i;
       const int64_t ps = pslot[e];
       if (C) {
