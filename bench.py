@@ -547,6 +547,9 @@ def run_single(args):
         "gpu_launches": int(plan.info.launches_mixed) * args.steps,
         "gpu_launches_per_step": int(plan.info.launches_mixed),
         "build_s": round(build_s, 3),
+        "tuned_scheme": (None if not getattr(plan, "tuned", None) else
+                         {"symmetric": int(plan.tuned[0]), "shape": int(plan.tuned[1])}),
+        "tuning_ms": (None if not f.tuning else {f"sym{k[0]}_shape{k[1]}": round(v, 3) for k, v in f.tuning.items()}),
         "fp64_ms_per_step": None if ms_fp64 is None else round(ms_fp64, 3),
         "mixed_over_fp64": None if ms_fp64 is None else round(ms_fp64 / ms_step, 2),
         "err_mixed_vs_fp64_direct": err_mixed, "err_fp64_vs_fp64_direct": err_fp64, "ncheck": len(idx),

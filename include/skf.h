@@ -126,7 +126,9 @@ int skf_plan_apply_host(skf_plan* plan, const void* x_host, void* y_host, int32_
    default.  Used to cross-check the two kernels. */
 #define SKF_OPT_SCALAR_MIXED 1
 /* SKF_OPT_PACKED_SHAPE: block shape of the packed kernel, 0 = 4 warps x 1 row
-   pair per thread (default), 1 = 1 warp x 4 pairs, 2 = 2 warps x 2 pairs. */
+   pair per thread (default), 1 = 1 warp x 4 pairs, 2 = 2 warps x 2 pairs
+   (256-row work items); 3 = 1 warp x 1 pair on 64-row work items (boxes of
+   a few dozen to a few hundred entries waste fewer rows). */
 #define SKF_OPT_PACKED_SHAPE 2
 /* SKF_OPT_SYMMETRIC: 1 (default) = for symmetric point kernels with symmetric
    lists, evaluate each kernel block once for both directions; 0 = off. */

@@ -576,6 +576,13 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
           if (!p->scalar_mixed) {
             // packed kernel geometry: warps per block x row pairs per thread
             switch (p->x2_config) {
+              case 3: {
+                TransArgs32 bs = b;
+                bs.work_box = p->work32s.box;
+                bs.work_row = p->work32s.row;
+                if (p->work32s.n > 0) k_translate_f32x2<OP, 1, 1><<<p->work32s.n, 32, 0, st>>>(bs);
+                break;
+              }
               case 1: k_translate_f32x2<OP, 1, 4><<<p->work32.n, 32, 0, st>>>(b); break;
               case 2: k_translate_f32x2<OP, 2, 2><<<p->work32.n, 64, 0, st>>>(b); break;
               default: k_translate_f32x2<OP, 4, 1><<<p->work32.n, 128, 0, st>>>(b); break;
@@ -587,6 +594,13 @@ static void launch_translate(const skf_plan* p, bool mixed, cudaStream_t st) {
       if constexpr (OP == SKF_HELMHOLTZ_3D) {
         if (!p->scalar_mixed) {
           switch (p->x2_config) {
+            case 3: {
+              TransArgs32 bs = b;
+              bs.work_box = p->work32s.box;
+              bs.work_row = p->work32s.row;
+              if (p->work32s.n > 0) k_translate_helm_x2<1, 1><<<p->work32s.n, 32, 0, st>>>(bs);
+              break;
+            }
             case 1: k_translate_helm_x2<1, 4><<<p->work32.n, 32, 0, st>>>(b); break;
             case 2: k_translate_helm_x2<2, 2><<<p->work32.n, 64, 0, st>>>(b); break;
             default: k_translate_helm_x2<4, 1><<<p->work32.n, 128, 0, st>>>(b); break;

@@ -437,8 +437,9 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
       pairs += s * (d->box_off[b + 1] - d->box_off[b]);
     }
     p->pairs = pairs;
-    for (int pass = 0; pass < 2; ++pass) {
-      const int tile = pass == 0 ? kTransThreads * kRowsPerThreadF64 : kT32Threads * kRowsPerThreadF32;
+    for (int pass = 0; pass < 3; ++pass) {
+      // FP64 kernel tiles, 256-row mixed tiles, 64-row mixed tiles
+      const int tile = pass == 0 ? kTransThreads * kRowsPerThreadF64 : (pass == 1 ? kT32Threads * kRowsPerThreadF32 : 64);
       std::vector<std::pair<int64_t, std::pair<int32_t, int32_t>>> items;
       for (int b = 0; b < nb; ++b) {
         const int bs = (int)(d->box_off[b + 1] - d->box_off[b]);
@@ -455,7 +456,7 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
         wb[i] = items[i].second.first;
         wr[i] = items[i].second.second;
       }
-      WorkList& w = pass == 0 ? p->work64 : p->work32;
+      WorkList& w = pass == 0 ? p->work64 : (pass == 1 ? p->work32 : p->work32s);
       w.n = (int)items.size();
       if (w.n > 0) {
         SKF_TRY(upload(p, &w.box, wb.data(), wb.size()));
@@ -748,7 +749,7 @@ int skf_plan_set_option(skf_plan* p, int32_t option, int64_t value) {
       p->sym_shape = (int)value;
       return SKF_OK;
     case SKF_OPT_PACKED_SHAPE:
-      if (value < 0 || value > 2) return SKF_ERR_ARG;
+      if (value < 0 || value > 3) return SKF_ERR_ARG;
       p->x2_config = (int)value;
       return SKF_OK;
     default: return SKF_ERR_ARG;

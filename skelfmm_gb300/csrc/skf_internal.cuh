@@ -53,7 +53,7 @@ struct skf_plan {
   int op = 0, ndim = 3, nboxes = 0, nlevels = 0, root_level = 0;
   bool cplx = false;
   bool scalar_mixed = false;  // force the scalar FP32 translation kernel (comparison/testing)
-  int x2_config = 0;          // packed kernel: 0 = 4 warps x 1 pair, 1 = 1 x 4, 2 = 2 x 2
+  int x2_config = 0;          // packed kernel: 0 = 4 warps x 1 pair, 1 = 1 x 4, 2 = 2 x 2, 3 = 1 x 1 (64-row items)
   int sym_shape = 0;          // symmetric kernel tile shape (SKF_OPT_SYM_SHAPE)
   // symmetric translations (mixed path, symmetric point kernels, symmetric lists)
   bool sym_ok = false;  // usable for this plan
@@ -109,6 +109,7 @@ struct skf_plan {
   int32_t* list_src = nullptr;
   int8_t* list_kind = nullptr;
   skf::WorkList work64, work32, worksym, worksymw;
+  skf::WorkList work32s;  // 64-row tiles of the packed kernel's one-warp shape (small boxes)
   skf::WorkList red;  // partial reduction items: box, 256-entry chunk (in .row)
   std::vector<skf::LevelBoxes> levels;  // indexed by level
   // apply vectors (scalars; complex: 2 doubles per entry)

@@ -471,7 +471,8 @@ __global__ void __launch_bounds__(NW * 32) k_translate_f32x2(TransArgs32 a) {
   constexpr int D = OpTraits<OP>::kDim;
   constexpr bool LOG = (OP == SKF_LAPLACE_2D);
   constexpr int TS = kTileSrcF32;
-  static_assert(64 * NW * NP == 256, "work items are 256-row tiles");
+  // a work item is a tile of 64 * NW * NP rows (256, or 64 for the 1 x 1 shape)
+  static_assert(64 * NW * NP == 256 || (NW == 1 && NP == 1), "work items are 256- or 64-row tiles");
   __shared__ ulonglong2 s0[TS], s1[TS], s2[TS], s3[TS];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -640,7 +641,8 @@ __device__ __forceinline__ void hx2_tile(const ulonglong2* __restrict__ s0, cons
 template <int NW, int NP>
 __global__ void __launch_bounds__(NW * 32) k_translate_helm_x2(TransArgs32 a) {
   constexpr int TS = kTileSrcF32;
-  static_assert(64 * NW * NP == 256, "work items are 256-row tiles");
+  // a work item is a tile of 64 * NW * NP rows (256, or 64 for the 1 x 1 shape)
+  static_assert(64 * NW * NP == 256 || (NW == 1 && NP == 1), "work items are 256- or 64-row tiles");
   __shared__ ulonglong2 s0[TS], s1[TS], s2[TS], s3[TS], s4[TS], s5[TS];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

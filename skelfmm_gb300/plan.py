@@ -338,8 +338,9 @@ class Plan:
 
         Candidates: for real operators the source-split symmetric kernel
         (when the lists are symmetric) and the per-direction packed kernel's
-        4-warp shape; for Helmholtz 3D the block-barrier symmetric kernel's
-        64 and 32-source tiles and the packed kernel's 4-warp and 2-warp
+        4-warp shape (256-row items) and 1-warp shape (64-row items); for
+        Helmholtz 3D the block-barrier symmetric kernel's 64 and 32-source
+        tiles and the packed kernel's 4-warp, 2-warp and 1-warp/64-row
         shapes; with ``exhaustive`` every shape of both kernels.  Each
         candidate is timed once, then the two fastest ``reps`` times unless
         the fastest leads by more than 15 %.  Returns {(symmetric, shape):
@@ -349,9 +350,9 @@ class Plan:
         sym_ok = info.npairs_evaluated_mixed < info.npairs_fused
         if exhaustive:
             # shapes 4 and 5: the source-split Laplace kernel (grid, persistent queue)
-            sym_shapes, dir_shapes = (range(4) if self.is_complex else range(6)), range(3)
+            sym_shapes, dir_shapes = (range(4) if self.is_complex else range(6)), range(4)
         else:
-            sym_shapes, dir_shapes = ((0, 2), (0, 2)) if self.is_complex else ((4,), (0,))
+            sym_shapes, dir_shapes = ((0, 2), (0, 2, 3)) if self.is_complex else ((4,), (0, 3))
         cands = ([(1, sh) for sh in sym_shapes] if sym_ok else []) + [(0, sh) for sh in dir_shapes]
 
         def select(sym, shape):
