@@ -654,7 +654,9 @@ def run_batch(args):
                 "d2h_bytes_per_step": ntot * 8, "ms_per_step": round(e2e_s * 1e3, 3)},
         "gpu_launches": int(b.plan.info.launches_mixed) * args.steps,
         "gpu_launches_per_step": int(b.plan.info.launches_mixed),
-        "build_s": round(build_s, 3), "tuning_ms": {f"sym{k[0]}_shape{k[1]}": round(v, 3) for k, v in b.tuning.items()},
+        "build_s": round(build_s, 3),
+        "build_phases_s": {k: round(v, 3) for k, v in b.build_phases_seconds.items()},
+        "tuning_ms": {f"sym{k[0]}_shape{k[1]}": round(v, 3) for k, v in b.tuning.items()},
         "err_max_f64_charges": float(errs.max()), "err_median_f64_charges": float(np.median(errs)),
         "err_max_f32_charges": float(errs32.max()), "ncheck_per_instance": 200,
         "roofline": roofline, "clocks": clk.summary(), "cpu_baseline": cpu,
@@ -715,6 +717,9 @@ def run_clusters(args):
             out[learned] = {
                 "build_s": round(bt, 3), "tree_s": round(f.tree_time_seconds, 3),
                 "skel_s": round(f.skel_time_seconds, 3), "setup_s": round(f.setup_time_seconds, 3),
+                "setup_phases_s": {k: round(v, 3) for k, v in f.setup_phases_seconds.items()},
+                "tuning_ms": None if not f.tuning else {f"sym{k[0]}_shape{k[1]}": round(v, 3)
+                                                        for k, v in f.tuning.items()},
                 "err_mixed": errs["mixed"], "err_fp64": errs["fp64"], "rank_max": int(f.rank_max),
                 "rank_mean": round(float(f.fmm.rank_list[sk].mean()), 2),
                 "mixed_apply_ms": round(ev0.elapsed_time(ev1) / 5, 3),

@@ -302,6 +302,15 @@ int skf_morton_keys(int32_t ndim, int64_t n, const double* x, const double* corn
                     uint64_t* keys, int64_t* q, void* stream);
 
 /*
+ * Stable ascending sort of n keys (DEVICE) on their low `bits` bits:
+ * keys_out (DEVICE [n]) and perm_out (DEVICE [n] int64, the input index of
+ * each output key; equal keys keep their input order).  The tree's point
+ * order (the point sort of simpletree.BalancedTree, skelfmm/skel_fmm.py:150).
+ */
+int skf_sort_keys(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, int64_t* perm_out, int32_t bits,
+                  void* stream);
+
+/*
  * Box levels and neighbour tables of the adaptive 2:1-balanced tree (the
  * tree the reference takes from simpletree.BalancedTree, called at
  * skelfmm/skel_fmm.py:150; its lists are read at

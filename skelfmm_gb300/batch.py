@@ -15,6 +15,7 @@ per-direction) and the packed kernel's block shape by timing them.
 from __future__ import annotations
 
 import ctypes
+from time import perf_counter
 
 import numpy as np
 import torch
@@ -180,25 +181,44 @@ class SkelFMMBatch:
         self.point_sets = [np.asarray(p, dtype=np.float64) for p in point_sets]
         self.geometries = geometries
         self.sizes = [int(p.shape[0]) for p in point_sets]
-        fmms = [RecursiveSkeletonization(BalancedTree(pts, leaf_size, device="cuda"), operator, param, tol,
+        ph = {}
+        t = perf_counter()
+
+        def lap(name):
+            nonlocal t
+            torch.cuda.synchronize()
+            now = perf_counter()
+            ph[name] = now - t
+            t = now
+
+        trees = [BalancedTree(pts, leaf_size, device="cuda") for pts in self.point_sets]
+        lap("trees")
+        fmms = [RecursiveSkeletonization(tree, operator, param, tol,
                                          geometry=None if geometries is None else geometries[i])
-                for i, pts in enumerate(self.point_sets)]
+                for i, tree in enumerate(trees)]
         if lockstep:
             skel_trees_lockstep(fmms, npoints_max)
         else:
             for fmm in fmms:
                 fmm.skel_tree(npoints_max=npoints_max)
+        lap("ids")
         rbs = []
         for fmm in fmms:
             fmm.setup_lists()
             rbs.append(fmm.ragged())
         self.instance_ragged = rbs
         self.ragged, self.starts = concat_ragged(rbs)
+        lap("lists")
         self.plan = Plan(self.ragged)
+        lap("plan")
         self.N = int(self.starts[-1])
         self.cplx = is_complex_op(operator)
         self._prec = _lib.PREC_MIXED if precision == "mixed" else _lib.PREC_FP64
         self.tuning = autotune(self.plan, self._prec) if (tune and self._prec != _lib.PREC_FP64) else None
+        lap("autotune")
+        # build phases (s): device trees, lockstep IDs, lists + concatenation,
+        # plan creation, autotuning
+        self.build_phases_seconds = ph
         dt = torch.complex128 if self.cplx else torch.float64
         self._x = torch.zeros(self.N, dtype=dt, device="cuda")
         self._y = torch.zeros(self.N, dtype=dt, device="cuda")

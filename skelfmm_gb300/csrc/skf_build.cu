@@ -132,6 +132,9 @@ struct SkelArgs {
   // deferred fallback: a rejected randomized ID writes only its status and
   // residual; its pivoted-QR ID runs in a second launch over the rejects
   int defer;
+  // sketch round of a randomized launch (1: the predicted rank, 2: the
+  // doubled sketch a first-round reject retries with), in the status code
+  int round;
   // set to 1 by any block whose proxy matrix has a non-finite entry or whose
   // points (normals) are not finite; NULL: unchecked
   int* nonfinite;
@@ -786,7 +789,7 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
     double* Y = A + (int64_t)m * n * W;
     const int guard = max(2, a.oversample / 2);
     bool ok = false;
-    const int rounds = 1;
+    const int rounds = a.round > 0 ? a.round : 1;
     {
       for (int64_t idx = threadIdx.x; idx < (int64_t)s * n; idx += blockDim.x) {
         const int j = (int)(idx / s), t = (int)(idx % s);
@@ -1297,7 +1300,7 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kSkelThre
         done = resid <= a.resid_tol;
         cl.sync();  // remote reads of pub done before it is reused
       }
-      code = (int8_t)(10 + (done ? 1 : 2));
+      code = (int8_t)(10 * (a.round > 0 ? a.round : 1) + (done ? 1 : 2));
     }
   }
   if (!done) {
@@ -1457,11 +1460,21 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
   // the sketch rank of a box is its predicted rank capped at its size (the
   // kernels apply the same cap)
   for (int b = 0; b < (int)hk.size(); ++b) hk[b] = (int32_t)std::min<int64_t>(hk[b], hoff[b + 1] - hoff[b]);
-  // workspace rows per box: K, plus the sketch when the box is randomized
+  // A first-round reject retries once with a doubled sketch (rank 2 k +
+  // oversample, capped at the box size) when that still fits; hk2 = 0: no
+  // retry.
+  std::vector<int32_t> hk2(hk.size(), 0);
+  for (int b = 0; b < (int)hk.size(); ++b) {
+    if (hk[b] <= 0 || !sketch_fits(hk[b] + ra.oversample, mrows)) continue;
+    const int64_t n = hoff[b + 1] - hoff[b];
+    const int32_t k2 = (int32_t)std::min<int64_t>(2 * (int64_t)hk[b] + ra.oversample, n);
+    if (k2 > hk[b] && sketch_fits(k2 + ra.oversample, mrows)) hk2[b] = k2;
+  }
+  // workspace rows per box: K, plus the (retry's) sketch when the box is randomized
   auto box_rows = [&](int b) -> int64_t {
     if (!ra.kpred || hk[b] <= 0) return mrows;
-    const int64_t s = (int64_t)hk[b] + ra.oversample;
-    return sketch_fits(s, mrows) ? mrows + s : mrows;  // K and the sketch
+    const int64_t s = (int64_t)std::max(hk[b], hk2[b]) + ra.oversample;
+    return sketch_fits((int64_t)hk[b] + ra.oversample, mrows) ? mrows + s : mrows;  // K and the sketch
   };
 
   double* dtmpl = nullptr;
@@ -1474,7 +1487,8 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
   if (ra.kpred) {
     int sk_rows = 1;
     for (int b = 0; b < nbox; ++b)
-      if (hk[b] > 0 && sketch_fits(hk[b] + ra.oversample, mrows)) sk_rows = std::max<int>(sk_rows, hk[b] + ra.oversample);
+      if (hk[b] > 0 && sketch_fits(hk[b] + ra.oversample, mrows))
+        sk_rows = std::max<int>(sk_rows, std::max(hk[b], hk2[b]) + ra.oversample);
     tab.resize((size_t)sk_rows * ra.rho);
     std::mt19937_64 gen(ra.seed);
     for (auto& e : tab) {
@@ -1502,12 +1516,25 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     }
   }
 
+  int32_t* dk2 = nullptr;  // retry sketch ranks
+  if (ra.kpred && nbox > 0) {
+    SKF_CUDA_TRY(cudaMallocAsync(&dk2, sizeof(int32_t) * nbox, st));
+    SKF_CUDA_TRY(cudaMemcpyAsync(dk2, hk2.data(), sizeof(int32_t) * nbox, cudaMemcpyHostToDevice, st));
+  }
+
   int* dbad = nullptr;  // non-finite proxy entries seen by any block
   SKF_CUDA_TRY(cudaMallocAsync(&dbad, sizeof(int), st));
   SKF_CUDA_TRY(cudaMemsetAsync(dbad, 0, sizeof(int), st));
 
-  // workspace in batches of boxes bounded by ~4 GiB
-  const int64_t budget = (int64_t)4 << 30;
+  // workspace in batches of boxes bounded by a quarter of the free device
+  // memory, at most 16 GiB (a level in one batch has one launch tail, not
+  // one per batch), at least 1 GiB
+  int64_t budget = (int64_t)4 << 30;
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+      budget = std::max<int64_t>((int64_t)1 << 30, std::min<int64_t>((int64_t)16 << 30, (int64_t)(free_b / 4)));
+  }
   int status = SKF_OK;
   cudaStream_t side = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1529,9 +1556,10 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
       return ra.kpred && hk[b] > 0 && sketch_fits(hk[b] + ra.oversample, mrows);
     };
     // cost ~ rows x n x min(rows, n), rows = the sketch or the proxy matrix
+    const std::vector<int32_t>* cost_k = &hk;  // sketch ranks of the launch being ordered
     auto box_cost = [&](int b, bool sketch) {
       const double n = (double)(hoff[b + 1] - hoff[b]);
-      const double rows = sketch ? (double)hk[b] + ra.oversample : (double)mrows;
+      const double rows = sketch ? (double)(*cost_k)[b] + ra.oversample : (double)mrows;
       return rows * n * std::min(rows, n);
     };
     double* ws = nullptr;
@@ -1651,11 +1679,33 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
           set_last_cuda_error(ce);
           status = SKF_ERR_CUDA;
         }
+        std::vector<int32_t> retry;
         for (int32_t lb : rnd)
-          if (hs[lb] % 10 == 2 && !done[lb]) full.push_back(lb);
+          if (hs[lb] % 10 == 2 && !done[lb]) (hk2[b0 + lb] > 0 ? retry : full).push_back(lb);
+        if (status == SKF_OK && !retry.empty()) {
+          // phase 2: the rejects retry with the doubled sketch
+          SkelArgs r2 = r;
+          r2.kpred = dk2;
+          r2.round = 2;
+          std::vector<int32_t> clustered2;
+          cost_k = &hk2;
+          status = launch_list(r2, retry, true, dord + nb, &clustered2);
+          cost_k = &hk;
+          if (status == SKF_OK) {
+            for (int32_t lb : clustered2) done[lb] = 1;
+            ce = cudaMemcpyAsync(hs.data(), dstat + b0, nb, cudaMemcpyDeviceToHost, st);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+            if (ce != cudaSuccess) {
+              set_last_cuda_error(ce);
+              status = SKF_ERR_CUDA;
+            }
+            for (int32_t lb : retry)
+              if (hs[lb] % 10 == 2 && !done[lb]) full.push_back(lb);
+          }
+        }
       }
     }
-    // phase 2: pivoted-QR IDs of the other boxes and of the rejects
+    // phase 3: pivoted-QR IDs of the other boxes and of the rejects
     if (status == SKF_OK) status = launch_list(a, full, false, dord + nb);
     cudaFreeAsync(ws, st);
     cudaFreeAsync(dwso, st);
@@ -1674,6 +1724,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
     }
   }
   cudaFreeAsync(dbad, st);
+  if (dk2) cudaFreeAsync(dk2, st);
   cudaFreeAsync(dtmpl, st);
   if (dtab) cudaFreeAsync(dtab, st);
   if (own_stat) cudaFreeAsync(own_stat, st);

@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include <algorithm>
 #include <memory>
 #include <new>
@@ -50,6 +52,44 @@ __global__ void k_morton_keys(int ndim, int64_t n, const double* __restrict__ x,
 }
 
 }  // namespace skf
+
+namespace skf {
+__global__ void k_iota64(int64_t n, int64_t* v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+}  // namespace skf
+
+// Stable sort of the point keys (LSD radix sort over the low `bits` bits,
+// CUB, compiled for this GPU): keys_out ascending, perm_out[i] = the input
+// index of keys_out[i] (equal keys keep their input order).
+extern "C" int skf_sort_keys(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, int64_t* perm_out, int32_t bits,
+                             void* stream) {
+  if (n < 0 || n > INT32_MAX || bits < 1 || bits > 64) return SKF_ERR_ARG;
+  if (n == 0) return SKF_OK;
+  if (!keys_in || !keys_out || !perm_out) return SKF_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int64_t* iota = nullptr;
+  void* tmp = nullptr;
+  size_t tmp_bytes = 0;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys_in, keys_out, (const int64_t*)nullptr,
+                                                  perm_out, (int)n, 0, bits, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&iota, sizeof(int64_t) * (size_t)n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&tmp, std::max<size_t>(tmp_bytes, 1), st);
+  if (e == cudaSuccess) {
+    skf::k_iota64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, iota);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys_in, keys_out, iota, perm_out, (int)n, 0, bits, st);
+  if (tmp) cudaFreeAsync(tmp, st);
+  if (iota) cudaFreeAsync(iota, st);
+  if (e != cudaSuccess) {
+    skf::set_last_cuda_error(e);
+    return e == cudaErrorMemoryAllocation ? SKF_ERR_OOM : SKF_ERR_CUDA;
+  }
+  return SKF_OK;
+}
 
 extern "C" int skf_morton_keys(int32_t ndim, int64_t n, const double* x, const double* corner, double L0,
                                int32_t depth, uint64_t* keys, int64_t* q, void* stream) {

@@ -343,8 +343,9 @@ class Plan:
         tiles and the packed kernel's 4-warp, 2-warp and 1-warp/64-row
         shapes; with ``exhaustive`` every shape of both kernels.  Each
         candidate is timed once, then the two fastest ``reps`` times unless
-        the fastest leads by more than 15 %.  Returns {(symmetric, shape):
-        ms}; the choice is kept in ``self.tuned``."""
+        the fastest leads by more than 15 %.  The 64-row shape is a candidate
+        only where its items evaluate at least 20 % fewer rows.  Returns
+        {(symmetric, shape): ms}; the choice is kept in ``self.tuned``."""
         self.set_option(_lib.OPT_SYMMETRIC, 1)
         info = self._query()
         sym_ok = info.npairs_evaluated_mixed < info.npairs_fused
@@ -353,14 +354,24 @@ class Plan:
             sym_shapes, dir_shapes = (range(4) if self.is_complex else range(6)), range(4)
         else:
             sym_shapes, dir_shapes = ((0, 2), (0, 2, 3)) if self.is_complex else ((4,), (0, 3))
+        if not exhaustive and 3 in dir_shapes and self._row_gain_64() < 1.25:
+            # 64-row items evaluate too few rows less than 256-row items to pay
+            dir_shapes = tuple(sh for sh in dir_shapes if sh != 3)
         cands = ([(1, sh) for sh in sym_shapes] if sym_ok else []) + [(0, sh) for sh in dir_shapes]
 
         def select(sym, shape):
             self.set_option(_lib.OPT_SYMMETRIC, sym)
             self.set_option(_lib.OPT_SYM_SHAPE if sym else _lib.OPT_PACKED_SHAPE, shape)
 
+        gain64 = self._row_gain_64() if (0, 3) in cands else 1.0
         results = {}
         for sym, shape in cands:
+            if (sym, shape) == (0, 3) and (0, 0) in results and results:
+                # 64-row items cut the 256-row shape's evaluated rows by
+                # gain64 at most, so they cannot beat a candidate already
+                # faster than the 256-row time / gain64
+                if min(results.values()) < results[(0, 0)] / gain64:
+                    continue
             select(sym, shape)
             key = (int(self.op), int(precision), sym, shape)
             if key not in _WARMED:
@@ -381,6 +392,20 @@ class Plan:
         self.info = self._query()
         self.tuned = best
         return results
+
+    def _row_gain_64(self):
+        """Rows a per-direction translation evaluates with 256-row work items
+        over those with 64-row items (each target box's rows padded to the
+        item, weighted by the entries of its list's sources)."""
+        rb = self.rb
+        bs = np.diff(np.asarray(rb.box_off, dtype=np.int64))
+        lo = np.asarray(rb.list_off, dtype=np.int64)
+        src = bs[np.asarray(rb.list_src, dtype=np.int64)]
+        csum = np.concatenate(([0], np.cumsum(src)))
+        S = (csum[lo[1:]] - csum[lo[:-1]]).astype(np.float64)
+        r256 = float(np.sum(-(-bs // 256) * 256 * S))
+        r64 = float(np.sum(-(-bs // 64) * 64 * S))
+        return r256 / r64 if r64 > 0 else 1.0
 
     def _query(self):
         info = _lib.PlanInfo()

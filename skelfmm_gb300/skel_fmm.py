@@ -192,13 +192,19 @@ class SkelFMM:
             self.skel_time_seconds = perf_counter() - t0
             t0 = perf_counter()
             fmm.setup_lists(verbose=verbose)
+            t1 = perf_counter()
             self.plan = Plan(fmm.ragged())
+            torch.cuda.synchronize(self.device)
+            t2 = perf_counter()
             self.tuning = None
             if self._prec_code != _lib.PREC_FP64 and self._autotune:
                 # translation scheme and tile shape for this plan, by timing them
                 self.tuning = self.plan.autotune(self._prec_code, reps=2)
             torch.cuda.synchronize(self.device)
-            self.setup_time_seconds = perf_counter() - t0
+            t3 = perf_counter()
+            self.setup_time_seconds = t3 - t0
+            # setup split: lists and index maps, plan creation, autotuning
+            self.setup_phases_seconds = {"lists": t1 - t0, "plan": t2 - t1, "autotune": t3 - t2}
         self.build_time_seconds = perf_counter() - t_build
         self.rank_max = fmm.rank_max
         self.fmm = fmm if self._keep_host_fmm else None

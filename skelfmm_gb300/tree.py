@@ -167,8 +167,8 @@ class BalancedTree:
     def _front_end_device(self, XX, device):
         """Root box, integer cells, keys and the stable key order computed on
         ``device``: skf_morton_keys (the same FP64 steps as the host path)
-        and a stable device sort (ties keep the input order).  Returns the
-        sorted keys (device)."""
+        and a stable device radix sort (skf_sort_keys; ties keep the input
+        order).  Returns the sorted keys (device)."""
         import torch
 
         from . import _lib
@@ -184,11 +184,14 @@ class BalancedTree:
         n, ndim = XX.shape
         ct = torch.from_numpy(np.ascontiguousarray(corner)).to(dev)
         keys = torch.empty(n, dtype=torch.int64, device=dev)
-        _lib.check(_lib.load().skf_morton_keys(ndim, n, _lib.ptr(x), _lib.ptr(ct), float(self.L0), self._depth,
-                                                _lib.ptr(keys), None,
-                                                torch.cuda.current_stream(dev).cuda_stream), "skf_morton_keys")
-        # keys < 2^63: the signed order is the unsigned one
-        skeys, perm = torch.sort(keys, stable=True)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        lib = _lib.load()
+        _lib.check(lib.skf_morton_keys(ndim, n, _lib.ptr(x), _lib.ptr(ct), float(self.L0), self._depth,
+                                       _lib.ptr(keys), None, stream), "skf_morton_keys")
+        skeys = torch.empty_like(keys)
+        perm = torch.empty(n, dtype=torch.int64, device=dev)
+        _lib.check(lib.skf_sort_keys(n, _lib.ptr(keys), _lib.ptr(skeys), _lib.ptr(perm), ndim * self._depth, stream),
+                   "skf_sort_keys")
         self._perm = perm.cpu().numpy()
         self._skeys = skeys.cpu().numpy().view(np.uint64)
         return skeys

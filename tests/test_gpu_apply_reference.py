@@ -164,3 +164,4 @@ def test_packed_block_shapes_agree(name):
         assert relinf(y, ys[0]) < 1e-6
     for y in ys:
         assert relinf(y, d["y_batched"]) < 2e-6
+
