@@ -107,6 +107,9 @@ typedef struct {
                                      (fewer than npairs_fused on the symmetric path) */
   int32_t launches_fp64;  /* kernel launches of one FP64 apply (memsets excluded) */
   int32_t launches_mixed; /* kernel launches of one mixed apply (memsets excluded) */
+  double rows_256_over_64; /* target rows a per-direction translation evaluates with
+                              256-row work items over those with 64-row items
+                              (rows padded per item, weighted by source entries) */
 } skf_plan_info;
 
 int skf_plan_create(const skf_plan_desc* desc, skf_plan** out);

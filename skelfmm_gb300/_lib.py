@@ -56,6 +56,7 @@ class PlanInfo(ctypes.Structure):
         ("nentries", _i64), ("npairs_fused", _i64), ("t_scalars", _i64),
         ("device_bytes", _i64), ("nwork", _i32), ("is_complex", _i32),
         ("npairs_evaluated_mixed", _i64), ("launches_fp64", _i32), ("launches_mixed", _i32),
+        ("rows_256_over_64", _f64),
     ]
 
 

@@ -133,7 +133,7 @@ struct SkelArgs {
   // residual; its pivoted-QR ID runs in a second launch over the rejects
   int defer;
   // sketch round of a randomized launch (1: the predicted rank, 2: the
-  // doubled sketch a first-round reject retries with), in the status code
+  // larger sketch a first-round reject retries with), in the status code
   int round;
   // set to 1 by any block whose proxy matrix has a non-finite entry or whose
   // points (normals) are not finite; NULL: unchecked
@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 2 : 1) k_skel_box(SkelArgs a) 
   bool done = false;
   if (sketch) {
     // ---- 2a. sketches Y = S K (s x n, after K in the workspace): row t of
-    // S has rho entries +-1 at hashed proxy rows; doubled while saturated
+    // S has rho entries +-1 at hashed proxy rows
     double* Y = A + (int64_t)m * n * W;
     const int guard = max(2, a.oversample / 2);
     bool ok = false;
@@ -1460,14 +1460,15 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
   // the sketch rank of a box is its predicted rank capped at its size (the
   // kernels apply the same cap)
   for (int b = 0; b < (int)hk.size(); ++b) hk[b] = (int32_t)std::min<int64_t>(hk[b], hoff[b + 1] - hoff[b]);
-  // A first-round reject retries once with a doubled sketch (rank 2 k +
-  // oversample, capped at the box size) when that still fits; hk2 = 0: no
-  // retry.
+  // A first-round reject retries once with a larger sketch (rank k +
+  // max(k / 2, 2 oversample), capped at the box size) when that still fits;
+  // hk2 = 0: no retry.
   std::vector<int32_t> hk2(hk.size(), 0);
   for (int b = 0; b < (int)hk.size(); ++b) {
     if (hk[b] <= 0 || !sketch_fits(hk[b] + ra.oversample, mrows)) continue;
     const int64_t n = hoff[b + 1] - hoff[b];
-    const int32_t k2 = (int32_t)std::min<int64_t>(2 * (int64_t)hk[b] + ra.oversample, n);
+    const int32_t k2 =
+        (int32_t)std::min<int64_t>((int64_t)hk[b] + std::max<int64_t>(hk[b] / 2, 2 * ra.oversample), n);
     if (k2 > hk[b] && sketch_fits(k2 + ra.oversample, mrows)) hk2[b] = k2;
   }
   // workspace rows per box: K, plus the (retry's) sketch when the box is randomized
@@ -1683,7 +1684,7 @@ static int skel_boxes_impl(int op, double kappa, int nbox, const int64_t* off, c
         for (int32_t lb : rnd)
           if (hs[lb] % 10 == 2 && !done[lb]) (hk2[b0 + lb] > 0 ? retry : full).push_back(lb);
         if (status == SKF_OK && !retry.empty()) {
-          // phase 2: the rejects retry with the doubled sketch
+          // phase 2: the rejects retry with the larger sketch
           SkelArgs r2 = r;
           r2.kpred = dk2;
           r2.round = 2;

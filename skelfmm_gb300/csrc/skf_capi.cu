@@ -6,10 +6,12 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -77,6 +79,22 @@ static int upload(skf_plan* p, T** dst, const T* src, size_t n) {
   }
   *dst = static_cast<T*>(d);
   return SKF_OK;
+}
+
+// f(lo, hi) over [0, n) split across up to 16 host threads (inline below
+// `grain` items per thread).
+template <class F>
+static void parallel_ranges(int64_t n, F&& f, int64_t grain = 1 << 15) {
+  const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+  const int nt = (int)std::min<int64_t>(std::min<int64_t>(hw, 16), (n + grain - 1) / grain);
+  if (nt <= 1) {
+    f((int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int t = 0; t < nt; ++t) th.emplace_back([&f, n, nt, t] { f(n * t / nt, n * (t + 1) / nt); });
+  for (auto& x : th) x.join();
 }
 
 static void free_plan(skf_plan* p) {
@@ -234,31 +252,38 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   const int nb = d->nboxes;
   const int64_t E = d->box_off[nb];
   if (E <= 0 || d->box_off[0] != 0) return SKF_ERR_ARG;
-  for (int b = 0; b < nb; ++b) {
-    const int64_t bs = d->box_off[b + 1] - d->box_off[b];
-    if (bs < 0 || d->box_rank[b] < 0 || d->box_rank[b] > bs) return SKF_ERR_ARG;
-    if (d->box_level[b] < 0 || d->box_level[b] >= d->nlevels) return SKF_ERR_ARG;
-  }
   if (d->nperm <= 0 || d->npoints <= 0) return SKF_ERR_ARG;
-  for (int64_t i = 0; i < d->nperm; ++i) {
-    if (d->perm_entry[i] < 0 || d->perm_entry[i] >= E || d->perm_point[i] < 0 || d->perm_point[i] >= d->npoints)
-      return SKF_ERR_ARG;
-  }
-  for (int64_t e = 0; e < E; ++e)
-    if (d->entry_pslot[e] < -1 || d->entry_pslot[e] >= E) return SKF_ERR_ARG;
   const int64_t L = d->list_off[nb];
   if (d->list_off[0] != 0 || L < 0) return SKF_ERR_ARG;
-  for (int64_t l = 0; l < L; ++l) {
-    if (d->list_src[l] < 0 || d->list_src[l] >= nb || d->list_kind[l] < 0 || d->list_kind[l] > 3) return SKF_ERR_ARG;
-  }
   const bool cplx = op_is_complex(d->op);
   const int W = cplx ? 2 : 1;
-  for (int b = 0; b < nb; ++b) {
-    const int64_t bs = d->box_off[b + 1] - d->box_off[b];
-    const int64_t r = d->box_rank[b];
-    if (r > 0 && d->box_level[b] > d->root_level) {
-      if (d->t_off[b] < 0 || d->t_off[b] + r * (bs - r) > d->t_len) return SKF_ERR_ARG;
-    }
+  {
+    // the description's index arrays, checked on the host threads
+    std::atomic<bool> bad{false};
+    parallel_ranges(nb, [&](int64_t lo, int64_t hi) {
+      for (int64_t b = lo; b < hi && !bad; ++b) {
+        const int64_t bs = d->box_off[b + 1] - d->box_off[b];
+        const int64_t r = d->box_rank[b];
+        if (bs < 0 || r < 0 || r > bs || d->box_level[b] < 0 || d->box_level[b] >= d->nlevels ||
+            d->list_off[b + 1] < d->list_off[b] ||
+            (r > 0 && d->box_level[b] > d->root_level && (d->t_off[b] < 0 || d->t_off[b] + r * (bs - r) > d->t_len)))
+          bad = true;
+      }
+    });
+    parallel_ranges(d->nperm, [&](int64_t lo, int64_t hi) {
+      for (int64_t i = lo; i < hi && !bad; ++i)
+        if (d->perm_entry[i] < 0 || d->perm_entry[i] >= E || d->perm_point[i] < 0 || d->perm_point[i] >= d->npoints)
+          bad = true;
+    });
+    parallel_ranges(E, [&](int64_t lo, int64_t hi) {
+      for (int64_t e = lo; e < hi && !bad; ++e)
+        if (d->entry_pslot[e] < -1 || d->entry_pslot[e] >= E) bad = true;
+    });
+    parallel_ranges(L, [&](int64_t lo, int64_t hi) {
+      for (int64_t l = lo; l < hi && !bad; ++l)
+        if (d->list_src[l] < 0 || d->list_src[l] >= nb || d->list_kind[l] < 0 || d->list_kind[l] > 3) bad = true;
+    });
+    if (bad) return SKF_ERR_ARG;
   }
 
   skf_plan* p = new skf_plan();
@@ -425,20 +450,31 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
 
   // translation work items: (target box, row tile), most expensive first
   {
-    int64_t pairs = 0;
     std::vector<int64_t> src_sum(nb, 0);
-    for (int b = 0; b < nb; ++b) {
-      int64_t s = 0;
-      for (int64_t l = d->list_off[b]; l < d->list_off[b + 1]; ++l) {
-        const int sb = d->list_src[l];
-        s += d->box_off[sb + 1] - d->box_off[sb];
+    parallel_ranges(nb, [&](int64_t lo, int64_t hi) {
+      for (int64_t b = lo; b < hi; ++b) {
+        int64_t s = 0;
+        for (int64_t l = d->list_off[b]; l < d->list_off[b + 1]; ++l) {
+          const int sb = d->list_src[l];
+          s += d->box_off[sb + 1] - d->box_off[sb];
+        }
+        src_sum[b] = s;
       }
-      src_sum[b] = s;
-      pairs += s * (d->box_off[b + 1] - d->box_off[b]);
+    }, 4096);
+    int64_t pairs = 0;
+    double r256 = 0.0, r64 = 0.0;
+    for (int b = 0; b < nb; ++b) {
+      const int64_t bs = d->box_off[b + 1] - d->box_off[b];
+      pairs += src_sum[b] * bs;
+      r256 += (double)((bs + 255) / 256 * 256) * (double)src_sum[b];
+      r64 += (double)((bs + 63) / 64 * 64) * (double)src_sum[b];
     }
     p->pairs = pairs;
-    for (int pass = 0; pass < 3; ++pass) {
-      // FP64 kernel tiles, 256-row mixed tiles, 64-row mixed tiles
+    p->rows_256_over_64 = r64 > 0.0 ? r256 / r64 : 1.0;
+    // FP64 kernel tiles, 256-row mixed tiles, 64-row mixed tiles: one host
+    // thread per list
+    std::vector<int32_t> wb[3], wr[3];
+    auto build_items = [&](int pass) {
       const int tile = pass == 0 ? kTransThreads * kRowsPerThreadF64 : (pass == 1 ? kT32Threads * kRowsPerThreadF32 : 64);
       std::vector<std::pair<int64_t, std::pair<int32_t, int32_t>>> items;
       for (int b = 0; b < nb; ++b) {
@@ -451,16 +487,25 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
       }
       std::stable_sort(items.begin(), items.end(),
                        [](const auto& a, const auto& b) { return a.first > b.first; });
-      std::vector<int32_t> wb(items.size()), wr(items.size());
+      wb[pass].resize(items.size());
+      wr[pass].resize(items.size());
       for (size_t i = 0; i < items.size(); ++i) {
-        wb[i] = items[i].second.first;
-        wr[i] = items[i].second.second;
+        wb[pass][i] = items[i].second.first;
+        wr[pass][i] = items[i].second.second;
       }
+    };
+    {
+      std::thread t1(build_items, 1), t2(build_items, 2);
+      build_items(0);
+      t1.join();
+      t2.join();
+    }
+    for (int pass = 0; pass < 3; ++pass) {
       WorkList& w = pass == 0 ? p->work64 : (pass == 1 ? p->work32 : p->work32s);
-      w.n = (int)items.size();
+      w.n = (int)wb[pass].size();
       if (w.n > 0) {
-        SKF_TRY(upload(p, &w.box, wb.data(), wb.size()));
-        SKF_TRY(upload(p, &w.row, wr.data(), wr.size()));
+        SKF_TRY(upload(p, &w.box, wb[pass].data(), wb[pass].size()));
+        SKF_TRY(upload(p, &w.row, wr[pass].data(), wr[pass].size()));
       }
     }
   }
@@ -494,41 +539,76 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
     }
     if (ok) {
       const int tile = kT32Threads * kRowsPerThreadF32;
-      std::vector<int64_t> soff(nb + 1, 0), poff, pbase(nb, 0), pstride(nb, 0);
-      std::vector<int32_t> ssrc;
-      std::vector<int8_t> skind;
-      // B-side partial blocks each box receives, as (box, block) in the
-      // order the reduction adds them, grouped into CSR below
-      std::vector<std::pair<int32_t, int64_t>> incoming;
+      // Two passes over the boxes on the host threads: counts (entries with
+      // B >= A, incoming partial blocks, work items), prefix sums, then
+      // every box fills its own ranges, in the order a single pass would.
+      std::vector<int64_t> cnt(nb), nin(nb), stride_v(nb), srcsum_v(nb), ntl(nb);
+      parallel_ranges(nb, [&](int64_t lo, int64_t hi) {
+        for (int64_t A = lo; A < hi; ++A) {
+          int64_t c = 0, cn = 0, stv = 0, ss = 0;
+          for (int64_t l = d->list_off[A]; l < d->list_off[A + 1]; ++l) {
+            const int B = d->list_src[l];
+            if (B < A) continue;
+            const int64_t bsB = d->box_off[B + 1] - d->box_off[B];
+            ++c;
+            if (B != A) {
+              ++cn;
+              stv += nparts * bsB;
+            }
+            ss += bsB;
+          }
+          const int64_t bsA = d->box_off[A + 1] - d->box_off[A];
+          const int64_t nt = bsA > 0 ? (bsA + tile - 1) / tile : 0;
+          cnt[A] = c;
+          nin[A] = nt * cn;
+          stride_v[A] = stv;
+          srcsum_v[A] = ss;
+          ntl[A] = nt;
+        }
+      }, 2048);
+      std::vector<int64_t> soff(nb + 1, 0), pbase(nb, 0), pstride(nb, 0), inb(nb + 1, 0), itb(nb + 1, 0);
       int64_t total = 0, sym_pairs = 0;
-      std::vector<std::pair<int64_t, std::pair<int32_t, int32_t>>> items;
       for (int A = 0; A < nb; ++A) {
         const int64_t bsA = d->box_off[A + 1] - d->box_off[A];
-        const size_t first = ssrc.size();
-        int64_t stride = 0, srcsum = 0;
-        for (int64_t l = d->list_off[A]; l < d->list_off[A + 1]; ++l) {
-          const int B = d->list_src[l];
-          if (B < A) continue;
-          const int64_t bsB = d->box_off[B + 1] - d->box_off[B];
-          ssrc.push_back(B);
-          skind.push_back(d->list_kind[l]);
-          poff.push_back(B == A ? 0 : stride);
-          if (B != A) stride += nparts * bsB;
-          srcsum += bsB;
-        }
-        soff[A + 1] = (int64_t)ssrc.size();
-        pstride[A] = stride;
+        soff[A + 1] = soff[A] + cnt[A];
         pbase[A] = total;
-        const int64_t ntiles = bsA > 0 ? (bsA + tile - 1) / tile : 0;
-        for (int64_t t = 0; t < ntiles; ++t)
-          for (size_t k = first; k < ssrc.size(); ++k)
-            if (ssrc[k] != A) incoming.push_back({ssrc[k], total + t * stride + poff[k]});
-        total += ntiles * stride;
-        sym_pairs += bsA * srcsum;
-        if (bsA > 0 && ssrc.size() > first)
-          for (int r0 = 0; r0 < bsA; r0 += tile)
-            items.push_back({std::min<int64_t>(tile, bsA - r0) * srcsum, {A, r0}});
+        pstride[A] = stride_v[A];
+        total += ntl[A] * stride_v[A];
+        sym_pairs += bsA * srcsum_v[A];
+        inb[A + 1] = inb[A] + nin[A];
+        itb[A + 1] = itb[A] + ((bsA > 0 && cnt[A] > 0) ? ntl[A] : 0);
       }
+      std::vector<int32_t> ssrc((size_t)soff[nb]);
+      std::vector<int8_t> skind((size_t)soff[nb]);
+      std::vector<int64_t> poff((size_t)soff[nb]);
+      // B-side partial blocks each box receives, as (box, block) in the
+      // order the reduction adds them, grouped into CSR below
+      std::vector<std::pair<int32_t, int64_t>> incoming((size_t)inb[nb]);
+      std::vector<std::pair<int64_t, std::pair<int32_t, int32_t>>> items((size_t)itb[nb]);
+      parallel_ranges(nb, [&](int64_t lo, int64_t hi) {
+        for (int64_t A = lo; A < hi; ++A) {
+          int64_t k = soff[A], stv = 0;
+          for (int64_t l = d->list_off[A]; l < d->list_off[A + 1]; ++l) {
+            const int B = d->list_src[l];
+            if (B < A) continue;
+            const int64_t bsB = d->box_off[B + 1] - d->box_off[B];
+            ssrc[k] = B;
+            skind[k] = d->list_kind[l];
+            poff[k] = B == A ? 0 : stv;
+            if (B != A) stv += nparts * bsB;
+            ++k;
+          }
+          int64_t o = inb[A];
+          for (int64_t t = 0; t < ntl[A]; ++t)
+            for (int64_t k2 = soff[A]; k2 < soff[A + 1]; ++k2)
+              if (ssrc[k2] != A) incoming[o++] = {ssrc[k2], pbase[A] + t * stride_v[A] + poff[k2]};
+          const int64_t bsA = d->box_off[A + 1] - d->box_off[A];
+          int64_t it = itb[A];
+          if (bsA > 0 && cnt[A] > 0)
+            for (int64_t r0 = 0; r0 < bsA; r0 += tile)
+              items[it++] = {std::min<int64_t>(tile, bsA - r0) * srcsum_v[A], {(int32_t)A, (int32_t)r0}};
+        }
+      }, 2048);
       std::stable_sort(items.begin(), items.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
       std::vector<int32_t> wb(items.size()), wr(items.size());
       for (size_t i = 0; i < items.size(); ++i) {
@@ -562,48 +642,71 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
       // contiguous parts, so the launch has enough items to fill the GPU.
       constexpr int kTileW = 32, kMaxParts = 8;
       std::vector<int32_t> ntil(nb, 0), npart(nb, 1);
-      std::vector<int64_t> apart(nb, -1);
+      std::vector<int64_t> apart(nb, -1), wc(nb, 0);
+      if (!cplx)
+        parallel_ranges(nb, [&](int64_t lo, int64_t hi) {
+          for (int64_t A = lo; A < hi; ++A) {
+            int64_t t = 0;
+            for (int64_t k = soff[A]; k < soff[A + 1]; ++k) {
+              const int B = ssrc[k];
+              const int kind = skind[k];
+              const int64_t bsB = d->box_off[B + 1] - d->box_off[B];
+              const int64_t nh = (kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_DOWN)
+                                     ? d->box_rank[B]
+                                     : (kind == SKF_KIND_COARSE_UP ? bsB : 0);
+              t += (nh + kTileW - 1) / kTileW + (bsB - nh + kTileW - 1) / kTileW;
+            }
+            ntil[A] = (int32_t)t;
+            wc[A] = (d->box_off[A + 1] - d->box_off[A]) * t;
+          }
+        }, 2048);
       int64_t wcost_total = 0;
-      for (int A = 0; A < nb && !cplx; ++A) {
-        int64_t t = 0;
-        for (int64_t k = soff[A]; k < soff[A + 1]; ++k) {
-          const int B = ssrc[k];
-          const int kind = skind[k];
-          const int64_t bsB = d->box_off[B + 1] - d->box_off[B];
-          const int64_t nh = (kind == SKF_KIND_COLLEAGUE || kind == SKF_KIND_COARSE_DOWN)
-                                 ? d->box_rank[B]
-                                 : (kind == SKF_KIND_COARSE_UP ? bsB : 0);
-          t += (nh + kTileW - 1) / kTileW + (bsB - nh + kTileW - 1) / kTileW;
-        }
-        ntil[A] = (int32_t)t;
-        wcost_total += (d->box_off[A + 1] - d->box_off[A]) * t;
-      }
+      for (int A = 0; A < nb; ++A) wcost_total += wc[A];
       // an even share for ~4 waves of 3 blocks per SM on 152 SMs
       const double share = (double)wcost_total / (152.0 * 3.0 * 4.0);
+      // parts per box, their A-side partial regions and item counts
       int64_t aoff = total;
-      std::vector<std::pair<int32_t, int64_t>> incoming_w = std::move(incoming);
-      std::vector<std::pair<int64_t, std::array<int32_t, 3>>> witems;
-      for (int A = 0; A < nb && !cplx; ++A) {
+      std::vector<int64_t> wib(nb + 1, 0), inw(nb + 1, 0);
+      for (int A = 0; A < nb; ++A) {
+        wib[A + 1] = wib[A];
+        inw[A + 1] = inw[A];
         const int64_t bsA = d->box_off[A + 1] - d->box_off[A];
-        if (bsA == 0 || ntil[A] == 0) continue;
+        if (cplx || bsA == 0 || ntil[A] == 0) continue;
         const double c = (double)std::min<int64_t>(tile, bsA) * ntil[A];
         int P = (int)std::min<double>(kMaxParts, std::max(1.0, std::ceil(c / std::max(share, 1.0))));
         P = std::min<int>(P, ntil[A]);
         npart[A] = P;
         if (P > 1) {
           apart[A] = aoff;
-          for (int q = 1; q < P; ++q) {
-            // hi and lo halves of the part's row sums: two incoming blocks
-            incoming_w.push_back({A, aoff + (int64_t)(q - 1) * 4 * bsA});
-            incoming_w.push_back({A, aoff + (int64_t)(q - 1) * 4 * bsA + 2 * bsA});
-          }
           aoff += (int64_t)(P - 1) * 4 * bsA;
+          inw[A + 1] += 2 * (int64_t)(P - 1);
         }
-        for (int r0 = 0; r0 < bsA; r0 += tile)
-          for (int q = 0; q < P; ++q)
-            witems.push_back({std::min<int64_t>(tile, bsA - r0) * ((int64_t)(q + 1) * ntil[A] / P - (int64_t)q * ntil[A] / P),
-                              {A, r0, q}});
+        wib[A + 1] += ((bsA + tile - 1) / tile) * P;
       }
+      const size_t n_in = incoming.size();
+      std::vector<std::pair<int32_t, int64_t>> incoming_w = std::move(incoming);
+      incoming_w.resize(n_in + (size_t)inw[nb]);
+      std::vector<std::pair<int64_t, std::array<int32_t, 3>>> witems((size_t)wib[nb]);
+      if (!cplx)
+        parallel_ranges(nb, [&](int64_t lo, int64_t hi) {
+          for (int64_t A = lo; A < hi; ++A) {
+            const int64_t bsA = d->box_off[A + 1] - d->box_off[A];
+            if (bsA == 0 || ntil[A] == 0) continue;
+            const int P = npart[A];
+            size_t o = n_in + (size_t)inw[A];
+            for (int q = 1; q < P; ++q) {
+              // hi and lo halves of the part's row sums: two incoming blocks
+              incoming_w[o++] = {(int32_t)A, apart[A] + (int64_t)(q - 1) * 4 * bsA};
+              incoming_w[o++] = {(int32_t)A, apart[A] + (int64_t)(q - 1) * 4 * bsA + 2 * bsA};
+            }
+            int64_t w = wib[A];
+            for (int64_t r0 = 0; r0 < bsA; r0 += tile)
+              for (int q = 0; q < P; ++q)
+                witems[w++] = {std::min<int64_t>(tile, bsA - r0) *
+                                   ((int64_t)(q + 1) * ntil[A] / P - (int64_t)q * ntil[A] / P),
+                               {(int32_t)A, (int32_t)r0, q}};
+          }
+        }, 2048);
       std::stable_sort(witems.begin(), witems.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
       std::vector<int32_t> wwb(witems.size()), wwr(witems.size()), wwq(witems.size());
       for (size_t i = 0; i < witems.size(); ++i) {
@@ -677,8 +780,11 @@ int skf_plan_create(const skf_plan_desc* d, skf_plan** out) {
   {
     // entry -> rank of its box, needed by the FP32 charge conversion
     std::vector<int32_t> er(E);
-    for (int b = 0; b < nb; ++b)
-      for (int64_t e = d->box_off[b]; e < d->box_off[b + 1]; ++e) er[e] = (int32_t)(e - d->box_off[b]) < d->box_rank[b] ? 1 : 0;
+    parallel_ranges(nb, [&](int64_t lo, int64_t hi) {
+      for (int64_t b = lo; b < hi; ++b)
+        for (int64_t e = d->box_off[b]; e < d->box_off[b + 1]; ++e)
+          er[e] = (int32_t)(e - d->box_off[b]) < d->box_rank[b] ? 1 : 0;
+    }, 1024);
     SKF_TRY(upload(p, &p->entry_skel, er.data(), (size_t)E));
   }
   cudaError_t e1 = cudaMemset(p->q, 0, sizeof(double) * E * W);
@@ -711,6 +817,7 @@ int skf_plan_query(const skf_plan* p, skf_plan_info* info) {
   for (int l = p->root_level + 1; l < p->nlevels; ++l) lv += p->levels[l].n > 0 ? 1 : 0;
   info->launches_fp64 = 2 + 2 * lv + (p->work64.n > 0 ? 1 : 0);
   info->launches_mixed = 2 + 2 * lv + 1 + (sym ? (p->worksym.n > 0 ? 1 : 0) + 1 : (p->work32.n > 0 ? 1 : 0));
+  info->rows_256_over_64 = p->rows_256_over_64;
   return SKF_OK;
 }
 

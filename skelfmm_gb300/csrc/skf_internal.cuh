@@ -84,6 +84,7 @@ struct skf_plan {
   double kappa = 0.0;
   int64_t E = 0, N = 0, nperm = 0, t_len = 0, nlist = 0;
   int64_t pairs = 0;  // kernel evaluations per apply
+  double rows_256_over_64 = 1.0;  // padded rows of 256-row over 64-row work items
 
   // per box
   int64_t* box_off = nullptr;

@@ -396,16 +396,9 @@ class Plan:
     def _row_gain_64(self):
         """Rows a per-direction translation evaluates with 256-row work items
         over those with 64-row items (each target box's rows padded to the
-        item, weighted by the entries of its list's sources)."""
-        rb = self.rb
-        bs = np.diff(np.asarray(rb.box_off, dtype=np.int64))
-        lo = np.asarray(rb.list_off, dtype=np.int64)
-        src = bs[np.asarray(rb.list_src, dtype=np.int64)]
-        csum = np.concatenate(([0], np.cumsum(src)))
-        S = (csum[lo[1:]] - csum[lo[:-1]]).astype(np.float64)
-        r256 = float(np.sum(-(-bs // 256) * 256 * S))
-        r64 = float(np.sum(-(-bs // 64) * 64 * S))
-        return r256 / r64 if r64 > 0 else 1.0
+        item, weighted by the entries of its list's sources; computed at plan
+        creation)."""
+        return float(self._query().rows_256_over_64)
 
     def _query(self):
         info = _lib.PlanInfo()

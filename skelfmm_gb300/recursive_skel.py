@@ -416,7 +416,13 @@ class RecursiveSkeletonization:
         def up(a):
             return torch.from_numpy(np.ascontiguousarray(a, dtype=np.int64)).to(dev)
 
-        col, crs, ch, lev = up(tree._colleagues), up(tree._coarse), up(tree._children), up(tree._box_level)
+        dt = getattr(tree, "_dev_tables", None)
+        tdev = None if dt is None else dt["colleagues"].device
+        if tdev is not None and tdev.type == dev.type and (dev.index is None or tdev.index == dev.index):
+            # the device tree's own tables
+            col, crs, ch, lev = dt["colleagues"], dt["coarse"], dt["children"], dt["level"]
+        else:
+            col, crs, ch, lev = up(tree._colleagues), up(tree._coarse), up(tree._children), up(tree._box_level)
         rb = up(self.root_boxes)
         nb = self.nboxes
         off = torch.empty(nb + 1, dtype=torch.int64, device=dev)

@@ -230,8 +230,18 @@ class BalancedTree:
             _lib.check(lib.skf_tree_export(h, *(_lib.ptr(a) for a in (
                 level_sep, code, coords, start, end, leaf, parent, children, colleagues, coarse)), stream),
                 "skf_tree_export")
+            # the neighbour tables also stay on the device for the lists
+            dev = skeys.device
+            dch = torch.empty((nb, nc), dtype=torch.int64, device=dev)
+            dco = torch.empty((nb, nq), dtype=torch.int64, device=dev)
+            dcr = torch.empty((nb, nc), dtype=torch.int64, device=dev)
+            _lib.check(lib.skf_tree_export(h, None, None, None, None, None, None, None, _lib.ptr(dch), _lib.ptr(dco),
+                                           _lib.ptr(dcr), stream), "skf_tree_export")
         finally:
             lib.skf_tree_destroy(h)
+        self._dev_tables = {"children": dch, "colleagues": dco, "coarse": dcr,
+                            "level": torch.repeat_interleave(torch.arange(nlev, dtype=torch.int64, device=dev),
+                                                             torch.from_numpy(np.diff(level_sep)).to(dev))}
         leaf = leaf.astype(bool)
         sl = [slice(int(level_sep[l]), int(level_sep[l + 1])) for l in range(nlev)]
         self._Lc = [coords[s] for s in sl]
