@@ -447,7 +447,9 @@ class RecursiveSkeletonization:
         root_boxes = np.hstack((tree.get_leaves_above(self.root_level),
                                 tree.get_boxes_level(self.root_level))).astype(np.int64)
         self.root_boxes = root_boxes
-        self.skel_leaves = np.setdiff1d(tree.get_leaves(), tree.get_leaves_above(self.root_level + 1))
+        leaves = tree.get_leaves()
+        # leaves at the root level or below (the sorted leaves minus those above)
+        self.skel_leaves = leaves[tree._box_level[leaves] > self.root_level]
         self.list_off, self.list_src, self.list_kind = self._lists_device()
 
         # entries: levels in order, boxes in order (levels above the root:
@@ -485,8 +487,8 @@ class RecursiveSkeletonization:
             fpos = t if self._final_pos[lev] is None else self._final_pos[lev][t]
             pslot[ebase[lev + 1] + cs[t]] = ebase[lev] + fpos
         self.entry_pslot = pslot
-        ent_leaf = np.repeat(leaf_mask, bs)
-        self.perm_entry = np.flatnonzero(ent_leaf).astype(np.int64)
+        # the entries of the leaves, in box order
+        self.perm_entry = _concat_ranges(off[:-1][leaves], bs[leaves])
         self.perm_point = ids[self.perm_entry]
         # T blocks: device buffers of the skeletonized levels, back to back
         cplx = is_complex_op(self.op_id)
