@@ -69,6 +69,36 @@ def test_invalid_arguments_are_rejected_before_any_device_work(lib):
                               None) == _lib.SKF_ERR_ARG
     assert lib.skf_skel_boxes_noalloc(1, 0.0, 0, None, None, None, None, 0.5, 400, 1e-6, None, None, None, None,
                                       None) == _lib.SKF_OK
+    # several trees in one launch: bad operator, missing per-box lengths, empty
+    assert lib.skf_skel_boxes_multi(42, 0.0, 1, None, None, None, None, None, 400, 1e-6, None, None, None, None,
+                                    None) == _lib.SKF_ERR_ARG
+    assert lib.skf_skel_boxes_multi(1, 0.0, 1, None, None, None, None, None, 400, 1e-6, None, None, None, None,
+                                    None) == _lib.SKF_ERR_ARG
+    assert lib.skf_skel_boxes_multi(1, 0.0, 0, None, None, None, None, None, 400, 1e-6, None, None, None, None,
+                                    None) == _lib.SKF_OK
+    # tree: dimension, depth (ndim x depth <= 63), leaf size, keys, output handle
+    t = ctypes.c_void_p()
+    for args in ((4, 10, 1, 20), (3, 10, 1, 22), (2, 10, 1, 0), (3, 0, 1, 20)):
+        nd, n, key, depth = args
+        assert lib.skf_tree_build(nd, n, ctypes.c_void_p(8) if key else None, depth, 16, ctypes.byref(t),
+                                  None) == _lib.SKF_ERR_ARG
+    assert lib.skf_tree_build(3, 10, None, 20, 16, ctypes.byref(t), None) == _lib.SKF_ERR_ARG
+    assert lib.skf_tree_build(3, 10, ctypes.c_void_p(8), 20, 0, ctypes.byref(t), None) == _lib.SKF_ERR_ARG
+    assert lib.skf_tree_build(3, 10, ctypes.c_void_p(8), 20, 16, None, None) == _lib.SKF_ERR_ARG
+    assert lib.skf_tree_query(None, None, None) == _lib.SKF_ERR_ARG
+    assert lib.skf_tree_export(None, *([None] * 11)) == _lib.SKF_ERR_ARG
+    lib.skf_tree_destroy(None)
+    # lists: dimension, root level, missing tables; sort: bit count, empty input
+    total = ctypes.c_int64()
+    assert lib.skf_lists_count(4, 10, None, None, None, None, 0, None, 0, None, ctypes.byref(total),
+                               None) == _lib.SKF_ERR_ARG
+    assert lib.skf_lists_count(3, 10, None, None, None, None, -1, None, 0, None, ctypes.byref(total),
+                               None) == _lib.SKF_ERR_ARG
+    assert lib.skf_lists_fill(3, 10, None, None, None, None, 0, None, 0, None, None, None, None) == _lib.SKF_ERR_ARG
+    assert lib.skf_sort_keys(10, None, None, None, 0, None) == _lib.SKF_ERR_ARG
+    assert lib.skf_sort_keys(10, None, None, None, 65, None) == _lib.SKF_ERR_ARG
+    assert lib.skf_sort_keys(0, None, None, None, 60, None) == _lib.SKF_OK
+    assert lib.skf_morton_keys(3, 10, None, None, 1.0, 22, None, None, None) == _lib.SKF_ERR_ARG
 
 
 def test_errors_map_to_python_exceptions():
