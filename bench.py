@@ -88,7 +88,53 @@ def parse():
     # keep the plan's default translation scheme instead of timing the
     # candidates (profiling runs, where ncu's serialisation skews the timings)
     p.add_argument("--no-autotune", action="store_true")
+    # the default run (default workload and sizes, with its CPU baseline)
+    # also measures the other workloads (C1, C3, C4, C5) in child processes
+    # after its own timed region, and reports them under
+    # "secondary_workloads"; --no-secondary skips that
+    p.add_argument("--no-secondary", action="store_true")
     return p.parse_args()
+
+
+SECONDARY = ("clusters_4M_learned", "batch64_annulus", "helmholtz3d_sphere_2M", "laplace2d_square_100k")
+
+
+def run_secondaries(budget_s=480.0, per_run_s=300.0):
+    """Each secondary workload in its own process (--no-cpu-baseline, 10
+    timed steps), after the default workload's timed region; returns a
+    compact summary of each line, or the reason it is missing."""
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE", "LOCAL_WORLD_SIZE", "MASTER_ADDR", "MASTER_PORT")}
+    out = {}
+    t0 = time.perf_counter()
+    for w in SECONDARY:
+        if time.perf_counter() - t0 > budget_s:
+            out[w] = {"skipped": "time budget of the default run"}
+            continue
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", w, "--no-cpu-baseline", "--no-secondary",
+               "--steps", "10", "--warmup", "3", "--fp64-steps", "1"]
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=per_run_s, env=env)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[w] = {"error": f"exit {r.returncode}: " + (r.stderr.strip().splitlines() or [""])[-1][:200]}
+                continue
+            d = json.loads(lines[-1])
+        except Exception as e:  # noqa: BLE001 - reported, never fatal to the default line
+            out[w] = {"error": f"{type(e).__name__}: {str(e)[:200]}"}
+            continue
+        keep = ("metric", "value", "unit", "ms_per_step", "build_s", "err_mixed_vs_fp64_direct", "err_max_f64_charges",
+                "tuned_scheme", "speedup_build", "speedup_ids", "clocks")
+        sm = {k: d[k] for k in keep if k in d and d[k] is not None}
+        if d.get("e2e"):
+            sm["e2e"] = d["e2e"].get("value")
+        if d.get("roofline"):
+            sm["roofline_frac"] = d["roofline"].get("frac")
+        for m in ("learned", "pivoted_qr"):
+            if m in d:
+                sm[m] = {k: d[m][k] for k in ("build_s", "skel_s", "setup_s", "err_mixed", "err_fp64") if k in d[m]}
+        out[w] = sm
+    return out
 
 
 def single_config(args):
@@ -556,6 +602,11 @@ def run_single(args):
         "roofline": roofline, "clocks": clocks,
         "cpu_baseline": cpu,
     }
+    if (rank == 0 and ws == 1 and args.workload == "laplace3d_cube_1M" and not args.no_secondary
+            and not args.no_cpu_baseline and args.n is None and args.tol is None and args.leaf is None):
+        del plan, f, xt, yt, flush
+        torch.cuda.empty_cache()
+        line["secondary_workloads"] = run_secondaries()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
