@@ -10,7 +10,7 @@ the build then computes a randomized ID at the predicted rank from a sketch
 of ``predicted rank + oversampling`` rows of the proxy matrix, checks it on
 rows of the full matrix, and falls back to the full pivoted-QR ID for the
 boxes whose check misses the tolerance (``RecursiveSkeletonization``).
-The pivoted-QR builds are both the training labels and the judge of the
+The pivoted-QR builds are both the training labels and the measure of the
 predictor's error.
 """
 

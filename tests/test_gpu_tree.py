@@ -128,3 +128,25 @@ def test_device_lists_equal_host_lists_at_every_root_level(case):
         g = fmm._lists_device()
         for a, b in zip(h, g):
             assert a.dtype == b.dtype and np.array_equal(a, b), (name, root)
+
+
+@pytest.mark.parametrize("bits", [60, 40, 9])
+def test_sort_keys_is_a_stable_sort(bits):
+    """skf_sort_keys against numpy's stable argsort, on keys with many ties
+    and keys using only the low ``bits`` bits."""
+    import torch
+
+    from skelfmm_gb300 import _lib
+
+    rng = np.random.default_rng(bits)
+    n = 300_001
+    keys = rng.integers(0, 1 << bits, n, dtype=np.uint64)
+    keys[::7] = keys[3]  # ties
+    k = torch.from_numpy(keys.view(np.int64)).cuda()
+    ko = torch.empty_like(k)
+    perm = torch.empty(n, dtype=torch.int64, device="cuda")
+    _lib.check(_lib.load().skf_sort_keys(n, _lib.ptr(k), _lib.ptr(ko), _lib.ptr(perm), bits,
+                                         torch.cuda.current_stream().cuda_stream), "skf_sort_keys")
+    ref = np.argsort(keys, kind="stable")
+    assert np.array_equal(perm.cpu().numpy(), ref)
+    assert np.array_equal(ko.cpu().numpy().view(np.uint64), keys[ref])
