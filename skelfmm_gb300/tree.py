@@ -108,7 +108,8 @@ class BalancedTree:
 
         D = _MAX_DEPTH[ndim]
         self._depth = D
-        if device is not None and str(device).startswith("cuda") and self.N >= DEVICE_FRONT_END_MIN_POINTS:
+        if (device is not None and str(device).startswith("cuda") and self.N >= DEVICE_FRONT_END_MIN_POINTS
+                and self.N < 2 ** 31):  # the device sort indexes points with 32-bit counts
             skeys = self._front_end_device(XX, device)
             self._box_levels_device(skeys)
             self._set_geometry()
