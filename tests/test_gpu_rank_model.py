@@ -187,6 +187,24 @@ def test_underpredicted_ranks_fall_back_to_pivoted_qr(reference_build):
     assert _apply_error(pts, plan) <= max(3 * err_full, 1e-6)
 
 
+def test_slightly_low_predictions_retry_with_a_larger_sketch(reference_build):
+    """Predictions 20 % below the pivoted-QR ranks: boxes whose first sketch
+    misses retry with a larger one (status 2x) and keep that ID instead of
+    falling back to the pivoted QR; the result meets the same tolerance."""
+    pts, f_full, err_full = reference_build
+
+    class Low:
+        def __call__(self, fmm, lev, boxes, x_lev, off):
+            return np.maximum(1, (0.8 * f_full.rank_list[boxes]).astype(np.int64))
+
+    _, f, plan = _cube_build(Low())
+    st = np.concatenate([v for v in f._status_by_lev.values()])
+    retried = st // 10 == 2
+    assert retried.sum() > 0
+    assert np.count_nonzero(retried & (st % 10 == 1)) > 0.5 * retried.sum()
+    assert _apply_error(pts, plan) <= max(3 * err_full, 1e-6)
+
+
 def test_network_gains_over_build_without_it(reference_build):
     """With the network's predictions most boxes keep their randomized ID;
     driven by a prediction-free guess (the same small rank for every box)
