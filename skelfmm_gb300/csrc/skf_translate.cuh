@@ -1115,7 +1115,7 @@ __device__ __forceinline__ void symw_tile(const ulonglong2* __restrict__ sb, int
                                           const f2_t (&c1T)[kSymwPairs], const f2_t (&c2T)[kSymwPairs],
                                           f2_t (&pu)[kSymwPairs], f2_t (&ph)[kSymwPairs], float* __restrict__ sTu,
                                           float* __restrict__ sTh) {
-#pragma unroll 2
+#pragma unroll 4
   for (int j = 0; j < nt; ++j) {
     const ulonglong2 A = sb[j];                     // (-hx,-hx), (-hy,-hy)
     const ulonglong2 B = sb[symw_ts() + j];         // (-hz,-hz), (-lx,-lx)
