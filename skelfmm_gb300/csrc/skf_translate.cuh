@@ -591,7 +591,7 @@ __device__ __forceinline__ void hx2_tile(const ulonglong2* __restrict__ s0, cons
                                          f2_t kc2, f2_t (&pur)[NP], f2_t (&pui)[NP], f2_t (&phr)[NP],
                                          f2_t (&phi)[NP]) {
   const f2_t two_pi = f2_pack(6.283185307179586f, 6.283185307179586f);
-#pragma unroll 2
+#pragma unroll 4
   for (int j = 0; j < nt; ++j) {
     const ulonglong2 A = s0[j];   // (-hx), (-hy)
     const ulonglong2 B = s1[j];   // (-hz), (-lx)
