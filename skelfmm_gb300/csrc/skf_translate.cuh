@@ -470,7 +470,9 @@ template <int OP, int NW, int NP>
 __global__ void __launch_bounds__(NW * 32) k_translate_f32x2(TransArgs32 a) {
   constexpr int D = OpTraits<OP>::kDim;
   constexpr bool LOG = (OP == SKF_LAPLACE_2D);
-  constexpr int TS = kTileSrcF32;
+  // 64-source tiles for the one-warp shape: 4 KB of staged sources per
+  // block, so more blocks fit an SM
+  constexpr int TS = (NW == 1 && NP == 1) ? 64 : kTileSrcF32;
   // a work item is a tile of 64 * NW * NP rows (256, or 64 for the 1 x 1 shape)
   static_assert(64 * NW * NP == 256 || (NW == 1 && NP == 1), "work items are 256- or 64-row tiles");
   __shared__ ulonglong2 s0[TS], s1[TS], s2[TS], s3[TS];
