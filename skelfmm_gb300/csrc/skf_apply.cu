@@ -342,15 +342,36 @@ __global__ void __launch_bounds__(256) k_down_ff(const int32_t* __restrict__ box
   const float* Tl = tlo + t_off[b] * W;
   for (int c = threadIdx.x; c < nred; c += blockDim.x) {
     FF ar, ai;
-    for (int i = 0; i < r; ++i) {
-      const int64_t k = ((int64_t)i * nred + c) * W;
-      if (C) {
+    if constexpr (C) {
+      // complex: two chains (even and odd rows) for independent work
+      FF br, bi;
+      int i = 0;
+      for (; i + 1 < r; i += 2) {
+        const int64_t k = ((int64_t)i * nred + c) * W, k2 = k + (int64_t)nred * W;
+        const float trh = Th[k], tih = Th[k + 1], trl = Tl[k], til = Tl[k + 1];
+        const float urh = Th[k2], uih = Th[k2 + 1], url = Tl[k2], uil = Tl[k2 + 1];
+        ff_add_prod(ar, trh, trl, hh[2 * i], hl[2 * i]);
+        ff_sub_prod(ar, tih, til, hh[2 * i + 1], hl[2 * i + 1]);
+        ff_add_prod(ai, trh, trl, hh[2 * i + 1], hl[2 * i + 1]);
+        ff_add_prod(ai, tih, til, hh[2 * i], hl[2 * i]);
+        ff_add_prod(br, urh, url, hh[2 * i + 2], hl[2 * i + 2]);
+        ff_sub_prod(br, uih, uil, hh[2 * i + 3], hl[2 * i + 3]);
+        ff_add_prod(bi, urh, url, hh[2 * i + 3], hl[2 * i + 3]);
+        ff_add_prod(bi, uih, uil, hh[2 * i + 2], hl[2 * i + 2]);
+      }
+      if (i < r) {
+        const int64_t k = ((int64_t)i * nred + c) * W;
         const float trh = Th[k], tih = Th[k + 1], trl = Tl[k], til = Tl[k + 1];
         ff_add_prod(ar, trh, trl, hh[2 * i], hl[2 * i]);
         ff_sub_prod(ar, tih, til, hh[2 * i + 1], hl[2 * i + 1]);
         ff_add_prod(ai, trh, trl, hh[2 * i + 1], hl[2 * i + 1]);
         ff_add_prod(ai, tih, til, hh[2 * i], hl[2 * i]);
-      } else {
+      }
+      ar = ff_add(ar, br);
+      ai = ff_add(ai, bi);
+    } else {
+      for (int i = 0; i < r; ++i) {
+        const int64_t k = (int64_t)i * nred + c;
         ff_add_prod(ar, Th[k], Tl[k], hh[i], hl[i]);
       }
     }
