@@ -201,17 +201,21 @@ class RecursiveSkeletonization:
         sb = sb[order]
         st = np.concatenate(seg_start)[order]
         sl = np.concatenate(seg_len)[order].astype(np.int64)
+        # idx addresses [point order | child level's ids]: gather from each
+        # part directly instead of concatenating them
         idx = _concat_ranges(st, sl)
-        src = np.concatenate((tree._perm.astype(np.int64),
-                              self._ids[lev + 1] if (lev + 1 < self.nlevels and self._ids[lev + 1] is not None)
-                              else np.zeros(0, np.int64)))
-        ids = src[idx]
+        from_child = idx >= self.N
+        ids = np.empty(idx.shape[0], dtype=np.int64)
+        pm = ~from_child
+        ids[pm] = tree._perm[idx[pm]]
+        if lev + 1 < self.nlevels and self._ids[lev + 1] is not None:
+            ids[from_child] = self._ids[lev + 1][idx[from_child] - self.N]
         bs = np.bincount(sb - ls, weights=sl, minlength=le - ls).astype(np.int64)
         off = np.zeros(le - ls + 1, dtype=np.int64)
         np.cumsum(bs, out=off[1:])
         self._ids[lev] = ids
         self._off[lev] = off
-        self._cand_src[lev] = np.where(idx >= self.N, idx - self.N, -1)
+        self._cand_src[lev] = np.where(from_child, idx - self.N, -1)
         self._final_pos[lev] = None
         self.bs_list[ls:le] = bs
 
