@@ -366,6 +366,27 @@ int skf_lists_fill(int32_t ndim, int64_t nboxes, const int64_t* colleagues, cons
                    const int64_t* children, const int64_t* box_level, int32_t root_level, const int64_t* root_boxes,
                    int64_t nroot, const int64_t* list_off, int32_t* list_src, int8_t* list_kind, void* stream);
 
+/*
+ * Level bookkeeping of the build (HOST arrays, no device work), the
+ * candidate and skeleton-order steps of skelfmm/recursive_skel.py:209-262,
+ * 264-324.  skf_level_candidates: for the nbl boxes of a level, a leaf's
+ * candidates are its points perm[box_start[b] .. box_end[b]), a parent's the
+ * skeletons of its children in child order (children [nbl x nc], global box
+ * ids, -1 padded; child c's skeleton = child_ids[child_off[c -
+ * child_first_box] ..][:rank[c]]; child_ids NULL: the child level is not
+ * skeletonized and parents have none).  Writes off_out [nbl + 1] and *total;
+ * with ids_out non-NULL also ids_out [total] and cand_src_out [total] (the
+ * child-level entry each candidate comes from, -1 for points).
+ * skf_level_reorder: ids_out[off[b] + j] = ids_in[off[b] + perm[off[b] + j]]
+ * (perm box-local) and final_pos[off[b] + perm[off[b] + j]] = off[b] + j.
+ */
+int skf_level_candidates(int64_t nbl, const uint8_t* is_leaf, const int64_t* box_start, const int64_t* box_end,
+                         const int64_t* children, int32_t nc, int64_t child_first_box, const int64_t* child_off,
+                         const int64_t* child_ids, const int64_t* rank, const int64_t* perm, int64_t npoints,
+                         int64_t* off_out, int64_t* ids_out, int64_t* cand_src_out, int64_t* total);
+int skf_level_reorder(int64_t nbl, const int64_t* off, const int32_t* perm, const int64_t* ids_in, int64_t* ids_out,
+                      int64_t* final_pos);
+
 const char* skf_status_string(int32_t status);
 int skf_version(void);
 

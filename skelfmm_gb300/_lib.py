@@ -81,6 +81,8 @@ SIGNATURES = {
     "skf_box_moments": (_i32, [_i32, _i32, _p, _p, _p, _f64, _p, _p]),
     "skf_morton_keys": (_i32, [_i32, _i64, _p, _p, _f64, _i32, _p, _p, _p]),
     "skf_sort_keys": (_i32, [_i64, _p, _p, _p, _i32, _p]),
+    "skf_level_candidates": (_i32, [_i64, _p, _p, _p, _p, _i32, _i64, _p, _p, _p, _p, _i64, _p, _p, _p, _p]),
+    "skf_level_reorder": (_i32, [_i64, _p, _p, _p, _p, _p]),
     "skf_tree_build": (_i32, [_i32, _i64, _p, _i32, _i64, _p, _p]),
     "skf_tree_query": (_i32, [_p, _p, _p]),
     "skf_tree_export": (_i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),

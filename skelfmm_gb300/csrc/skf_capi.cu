@@ -938,4 +938,82 @@ int skf_skel_boxes_randomized(int32_t op, double kappa, int32_t nbox, const int6
                                static_cast<cudaStream_t>(stream));
 }
 
+// ---- level bookkeeping of the build (host, no device work) --------------
+
+int skf_level_candidates(int64_t nbl, const uint8_t* is_leaf, const int64_t* box_start, const int64_t* box_end,
+                         const int64_t* children, int32_t nc, int64_t child_first_box, const int64_t* child_off,
+                         const int64_t* child_ids, const int64_t* rank, const int64_t* perm, int64_t npoints,
+                         int64_t* off_out, int64_t* ids_out, int64_t* cand_src_out, int64_t* total) {
+  if (nbl < 0 || nc < 1 || nc > 8 || !is_leaf || !box_start || !box_end || !children || !rank || !perm || !off_out ||
+      !total || (child_ids && !child_off))
+    return SKF_ERR_ARG;
+  // sizes: a leaf holds its points; a parent the skeletons of its children
+  // (in child order), when the child level is skeletonized
+  std::vector<int64_t> sz((size_t)nbl, 0);
+  parallel_ranges(nbl, [&](int64_t lo, int64_t hi) {
+    for (int64_t b = lo; b < hi; ++b) {
+      if (is_leaf[b]) {
+        sz[b] = box_end[b] - box_start[b];
+      } else if (child_ids) {
+        int64_t t = 0;
+        for (int k = 0; k < nc; ++k) {
+          const int64_t c = children[b * nc + k];
+          if (c >= 0) t += rank[c];
+        }
+        sz[b] = t;
+      }
+    }
+  }, 4096);
+  off_out[0] = 0;
+  for (int64_t b = 0; b < nbl; ++b) off_out[b + 1] = off_out[b] + sz[b];
+  *total = off_out[nbl];
+  if (!ids_out) return SKF_OK;  // sizes only
+  if (!cand_src_out) return SKF_ERR_ARG;
+  for (int64_t b = 0; b < nbl; ++b)
+    if (is_leaf[b] && (box_start[b] < 0 || box_end[b] > npoints)) return SKF_ERR_ARG;
+  parallel_ranges(nbl, [&](int64_t lo, int64_t hi) {
+    for (int64_t b = lo; b < hi; ++b) {
+      int64_t o = off_out[b];
+      if (is_leaf[b]) {
+        for (int64_t i = box_start[b]; i < box_end[b]; ++i, ++o) {
+          ids_out[o] = perm[i];
+          cand_src_out[o] = -1;
+        }
+      } else if (child_ids) {
+        for (int k = 0; k < nc; ++k) {
+          const int64_t c = children[b * nc + k];
+          if (c < 0) continue;
+          const int64_t c0 = child_off[c - child_first_box];
+          for (int64_t t = 0; t < rank[c]; ++t, ++o) {
+            ids_out[o] = child_ids[c0 + t];
+            cand_src_out[o] = c0 + t;
+          }
+        }
+      }
+    }
+  }, 1024);
+  return SKF_OK;
+}
+
+int skf_level_reorder(int64_t nbl, const int64_t* off, const int32_t* perm, const int64_t* ids_in, int64_t* ids_out,
+                      int64_t* final_pos) {
+  if (nbl < 0 || !off || !perm || !ids_in || !ids_out || !final_pos) return SKF_ERR_ARG;
+  std::atomic<bool> bad{false};
+  parallel_ranges(nbl, [&](int64_t lo, int64_t hi) {
+    for (int64_t b = lo; b < hi && !bad; ++b) {
+      const int64_t o = off[b], n = off[b + 1] - off[b];
+      for (int64_t j = 0; j < n; ++j) {
+        const int64_t p = perm[o + j];
+        if (p < 0 || p >= n) {
+          bad = true;
+          break;
+        }
+        ids_out[o + j] = ids_in[o + p];
+        final_pos[o + p] = o + j;
+      }
+    }
+  }, 1024);
+  return bad ? SKF_ERR_ARG : SKF_OK;
+}
+
 }  // extern "C"

@@ -175,7 +175,41 @@ class RecursiveSkeletonization:
     def _level_candidates(self, lev):
         """Entries of every box at ``lev`` before its ID: the points of a
         leaf, else the skeletons of its children in child order
-        (recursive_skel.py:209-262)."""
+        (recursive_skel.py:209-262); on the host threads of the library
+        (``skf_level_candidates``), the same arrays as
+        ``_level_candidates_numpy``."""
+        tree = self.tree
+        ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+        nbl = le - ls
+        lib = _lib.load()
+        child = lev + 1 < self.nlevels and self._ids[lev + 1] is not None
+        leaf = np.ascontiguousarray(tree._is_leaf[ls:le], dtype=np.uint8)
+        start = np.ascontiguousarray(tree._box_start[ls:le], dtype=np.int64)
+        end = np.ascontiguousarray(tree._box_end[ls:le], dtype=np.int64)
+        ch = np.ascontiguousarray(tree._children[ls:le], dtype=np.int64)
+        rank = np.ascontiguousarray(self.rank_list, dtype=np.int64)
+        perm = np.ascontiguousarray(tree._perm, dtype=np.int64)
+        coff = np.ascontiguousarray(self._off[lev + 1], dtype=np.int64) if child else None
+        cids = np.ascontiguousarray(self._ids[lev + 1], dtype=np.int64) if child else None
+        cfirst = int(tree.level_sep[lev + 1]) if child else 0
+        off = np.empty(nbl + 1, dtype=np.int64)
+        total = ctypes.c_int64()
+        args = (nbl, _lib.ptr(leaf), _lib.ptr(start), _lib.ptr(end), _lib.ptr(ch), int(ch.shape[1]), cfirst,
+                _lib.ptr(coff), _lib.ptr(cids), _lib.ptr(rank), _lib.ptr(perm), int(self.N), _lib.ptr(off))
+        _lib.check(lib.skf_level_candidates(*args, None, None, ctypes.byref(total)), "skf_level_candidates")
+        ids = np.empty(int(total.value), dtype=np.int64)
+        cand = np.empty(int(total.value), dtype=np.int64)
+        _lib.check(lib.skf_level_candidates(*args, _lib.ptr(ids), _lib.ptr(cand), ctypes.byref(total)),
+                   "skf_level_candidates")
+        self._ids[lev] = ids
+        self._off[lev] = off
+        self._cand_src[lev] = cand
+        self._final_pos[lev] = None
+        self.bs_list[ls:le] = np.diff(off)
+
+    def _level_candidates_numpy(self, lev):
+        """``_level_candidates`` with numpy (the arrays it is checked
+        against)."""
         tree = self.tree
         ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
         boxes = np.arange(ls, le, dtype=np.int64)
@@ -316,14 +350,15 @@ class RecursiveSkeletonization:
         dev = self.device
         cplx = is_complex_op(self.op_id)
         rank_h = np.asarray(rank_h).astype(np.int64)
-        perm_h = np.asarray(perm_h).astype(np.int64)
-        ids = self._ids[lev]
-        # skeleton-first ids, candidate -> final position
-        base = np.repeat(off[:-1], bs)
-        src = base + perm_h
-        self._ids[lev] = ids[src]
+        perm_h = np.ascontiguousarray(perm_h, dtype=np.int32)
+        ids = np.ascontiguousarray(self._ids[lev], dtype=np.int64)
+        # skeleton-first ids, candidate -> final position (host threads)
+        new_ids = np.empty_like(ids)
         fp = np.empty(ids.shape[0], dtype=np.int64)
-        fp[src] = np.arange(ids.shape[0], dtype=np.int64)
+        _lib.check(_lib.load().skf_level_reorder(nbl, _lib.ptr(np.ascontiguousarray(off, dtype=np.int64)),
+                                                 _lib.ptr(perm_h), _lib.ptr(ids), _lib.ptr(new_ids), _lib.ptr(fp)),
+                   "skf_level_reorder")
+        self._ids[lev] = new_ids
         self._final_pos[lev] = fp
         self.rank_list[ls:le] = rank_h
         # compact the T blocks
