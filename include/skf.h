@@ -386,6 +386,17 @@ int skf_level_candidates(int64_t nbl, const uint8_t* is_leaf, const int64_t* box
                          int64_t* off_out, int64_t* ids_out, int64_t* cand_src_out, int64_t* total);
 int skf_level_reorder(int64_t nbl, const int64_t* off, const int32_t* perm, const int64_t* ids_in, int64_t* ids_out,
                       int64_t* final_pos);
+/*
+ * Parent slots of the ragged build (the index maps of
+ * skelfmm/recursive_skel.py:714-780; HOST): pslot [nentries] = -1, then for
+ * every level l of nlev and candidate t of it with cand_src[l][t] = c >= 0,
+ * pslot[base_child[l] + c] = base_parent[l] + (final_pos[l] ? final_pos[l][t]
+ * : t).  skf_gather_i64: out[i] = src[idx[i]] (0 <= idx < nsrc).
+ */
+int skf_parent_slots(int32_t nlev, const int64_t* const* cand_src, const int64_t* const* final_pos,
+                     const int64_t* ncand, const int64_t* base_child, const int64_t* base_parent, int64_t nentries,
+                     int64_t* pslot);
+int skf_gather_i64(int64_t n, const int64_t* idx, const int64_t* src, int64_t nsrc, int64_t* out);
 
 const char* skf_status_string(int32_t status);
 int skf_version(void);

@@ -83,6 +83,8 @@ SIGNATURES = {
     "skf_sort_keys": (_i32, [_i64, _p, _p, _p, _i32, _p]),
     "skf_level_candidates": (_i32, [_i64, _p, _p, _p, _p, _i32, _i64, _p, _p, _p, _p, _i64, _p, _p, _p, _p]),
     "skf_level_reorder": (_i32, [_i64, _p, _p, _p, _p, _p]),
+    "skf_parent_slots": (_i32, [_i32, _p, _p, _p, _p, _p, _i64, _p]),
+    "skf_gather_i64": (_i32, [_i64, _p, _p, _i64, _p]),
     "skf_tree_build": (_i32, [_i32, _i64, _p, _i32, _i64, _p, _p]),
     "skf_tree_query": (_i32, [_p, _p, _p]),
     "skf_tree_export": (_i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),

@@ -1016,4 +1016,50 @@ int skf_level_reorder(int64_t nbl, const int64_t* off, const int32_t* perm, cons
   return bad ? SKF_ERR_ARG : SKF_OK;
 }
 
+int skf_parent_slots(int32_t nlev, const int64_t* const* cand_src, const int64_t* const* final_pos,
+                     const int64_t* ncand, const int64_t* base_child, const int64_t* base_parent, int64_t nentries,
+                     int64_t* pslot) {
+  if (nlev < 0 || nentries < 0 || !pslot || (nlev > 0 && (!cand_src || !final_pos || !ncand || !base_child ||
+                                                         !base_parent)))
+    return SKF_ERR_ARG;
+  parallel_ranges(nentries, [&](int64_t lo, int64_t hi) {
+    for (int64_t e = lo; e < hi; ++e) pslot[e] = -1;
+  });
+  std::atomic<bool> bad{false};
+  for (int l = 0; l < nlev; ++l) {
+    const int64_t* cs = cand_src[l];
+    const int64_t* fp = final_pos[l];
+    if (!cs || ncand[l] <= 0) continue;
+    parallel_ranges(ncand[l], [&](int64_t lo, int64_t hi) {
+      for (int64_t t = lo; t < hi; ++t) {
+        const int64_t c = cs[t];
+        if (c < 0) continue;
+        const int64_t dst = base_child[l] + c, val = base_parent[l] + (fp ? fp[t] : t);
+        if (dst < 0 || dst >= nentries || val < 0 || val >= nentries) {
+          bad = true;
+          return;
+        }
+        pslot[dst] = val;
+      }
+    });
+  }
+  return bad ? SKF_ERR_ARG : SKF_OK;
+}
+
+int skf_gather_i64(int64_t n, const int64_t* idx, const int64_t* src, int64_t nsrc, int64_t* out) {
+  if (n < 0 || (n > 0 && (!idx || !src || !out))) return SKF_ERR_ARG;
+  std::atomic<bool> bad{false};
+  parallel_ranges(n, [&](int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i) {
+      const int64_t j = idx[i];
+      if (j < 0 || j >= nsrc) {
+        bad = true;
+        return;
+      }
+      out[i] = src[j];
+    }
+  });
+  return bad ? SKF_ERR_ARG : SKF_OK;
+}
+
 }  // extern "C"

@@ -425,6 +425,37 @@ class RecursiveSkeletonization:
         for lev in range(self.root_level - 1, -1, -1):
             self._leaf_level_entries(lev)
 
+    def _parent_slots(self, ebase, nentries):
+        """Parent slots: skeleton entry i of child c sits at candidate
+        position t of its parent, which the parent's ID moved to
+        ``_final_pos`` (``skf_parent_slots`` on the library's host threads;
+        the same array as ``_parent_slots_numpy``)."""
+        levs = [lev for lev in range(self.root_level, self.nlevels - 1) if self._cand_src[lev] is not None]
+        keep = [(np.ascontiguousarray(self._cand_src[lev], dtype=np.int64),
+                 None if self._final_pos[lev] is None else np.ascontiguousarray(self._final_pos[lev], dtype=np.int64))
+                for lev in levs]
+        ptrs = ctypes.c_void_p * max(len(levs), 1)
+        cs_p = ptrs(*[k[0].ctypes.data for k in keep])
+        fp_p = ptrs(*[None if k[1] is None else k[1].ctypes.data for k in keep])
+        ncand = np.array([k[0].shape[0] for k in keep] or [0], dtype=np.int64)
+        bchild = np.array([ebase[lev + 1] for lev in levs] or [0], dtype=np.int64)
+        bparent = np.array([ebase[lev] for lev in levs] or [0], dtype=np.int64)
+        pslot = np.empty(nentries, dtype=np.int64)
+        _lib.check(_lib.load().skf_parent_slots(len(levs), cs_p, fp_p, _lib.ptr(ncand), _lib.ptr(bchild),
+                                                _lib.ptr(bparent), nentries, _lib.ptr(pslot)), "skf_parent_slots")
+        return pslot
+
+    def _parent_slots_numpy(self, ebase, nentries):
+        pslot = np.full(nentries, -1, dtype=np.int64)
+        for lev in range(self.root_level, self.nlevels - 1):
+            cs = self._cand_src[lev]
+            if cs is None:
+                continue
+            t = np.flatnonzero(cs >= 0)
+            fpos = t if self._final_pos[lev] is None else self._final_pos[lev][t]
+            pslot[ebase[lev + 1] + cs[t]] = ebase[lev] + fpos
+        return pslot
+
     def _lists_host(self):
         """The translation lists in CSR by target box, with numpy (the same
         lists as ``_lists_device``)."""
@@ -515,20 +546,14 @@ class RecursiveSkeletonization:
         self.box_off = off
         ids = np.concatenate(ids_all) if ids_all else np.zeros(0, np.int64)
         self.entry_pid = ids
-        # parent slots: skeleton entry i of child c sits at candidate position
-        # t of its parent, which the parent's ID moved to _final_pos
-        pslot = np.full(int(off[-1]), -1, dtype=np.int64)
-        for lev in range(self.root_level, self.nlevels - 1):
-            cs = self._cand_src[lev]
-            if cs is None:
-                continue
-            t = np.flatnonzero(cs >= 0)
-            fpos = t if self._final_pos[lev] is None else self._final_pos[lev][t]
-            pslot[ebase[lev + 1] + cs[t]] = ebase[lev] + fpos
+        pslot = self._parent_slots(ebase, int(off[-1]))
         self.entry_pslot = pslot
         # the entries of the leaves, in box order
         self.perm_entry = _concat_ranges(off[:-1][leaves], bs[leaves])
-        self.perm_point = ids[self.perm_entry]
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        self.perm_point = np.empty(self.perm_entry.shape[0], dtype=np.int64)
+        _lib.check(_lib.load().skf_gather_i64(self.perm_entry.shape[0], _lib.ptr(self.perm_entry), _lib.ptr(ids),
+                                              ids.shape[0], _lib.ptr(self.perm_point)), "skf_gather_i64")
         # T blocks: device buffers of the skeletonized levels, back to back
         cplx = is_complex_op(self.op_id)
         t_off = np.full(nb, -1, dtype=np.int64)

@@ -72,3 +72,44 @@ def test_native_level_bookkeeping_equals_numpy(case):
     total = ctypes.c_int64()
     assert lib.skf_level_candidates(1, None, None, None, None, 8, 0, None, None, None, None, 1, None, None, None,
                                     ctypes.byref(total)) == _lib.SKF_ERR_ARG
+
+
+@pytest.mark.parametrize("case", [("gaussian_clusters", 60000, 64), ("curvy_annulus", 40000, 50)])
+def test_native_parent_slots_and_gather_equal_numpy(case):
+    """skf_parent_slots and skf_gather_i64 against numpy on a stand-in build
+    (random ranks and pivot orders) skeletonized down to level 2."""
+    from skelfmm_gb300 import _lib
+    from skelfmm_gb300.tree import get_point_dist
+
+    name, n, leaf = case
+    f = _fake_build(get_point_dist(n, name, rng=np.random.default_rng(n)), leaf)
+    tree = f.tree
+    rng = np.random.default_rng(3)
+    f.root_level = 2
+    for lev in range(tree.nlevels - 1, f.root_level, -1):
+        f._level_candidates(lev)
+        ls, le = int(tree.level_sep[lev]), int(tree.level_sep[lev + 1])
+        off = f._off[lev]
+        bs = np.diff(off)
+        f.rank_list[ls:le] = np.minimum(bs, rng.integers(1, 30, le - ls))
+        perm = np.concatenate([rng.permutation(b) for b in bs]) if bs.size else np.zeros(0, np.int64)
+        src = np.repeat(off[:-1], bs) + perm
+        fp = np.empty(src.shape[0], dtype=np.int64)
+        fp[src] = np.arange(src.shape[0])
+        f._ids[lev] = f._ids[lev][src]
+        f._final_pos[lev] = fp
+    for lev in range(f.root_level, -1, -1):
+        f._level_candidates(lev)
+    # entry bases per level as the ragged build lays them out
+    ebase = np.zeros(tree.nlevels + 1, dtype=np.int64)
+    for lev in range(tree.nlevels):
+        ebase[lev + 1] = ebase[lev] + (0 if f._off[lev] is None else int(f._off[lev][-1]))
+    E = int(ebase[-1])
+    assert np.array_equal(f._parent_slots(ebase, E), f._parent_slots_numpy(ebase, E))
+    idx = rng.integers(0, E, 100000)
+    src = rng.integers(-5, 5, E)
+    out = np.empty(idx.shape[0], dtype=np.int64)
+    _lib.check(_lib.load().skf_gather_i64(idx.shape[0], _lib.ptr(idx), _lib.ptr(src), E, _lib.ptr(out)), "gather")
+    assert np.array_equal(out, src[idx])
+    idx[7] = E
+    assert _lib.load().skf_gather_i64(idx.shape[0], _lib.ptr(idx), _lib.ptr(src), E, _lib.ptr(out)) == _lib.SKF_ERR_ARG
